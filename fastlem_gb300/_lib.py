@@ -1,0 +1,107 @@
+"""ctypes binding of libfastlem_gb300.so (include/fastlem_gb300.h).
+
+There is no fallback: if the library is missing or cannot be loaded, every call
+raises.  Build it with `python -m fastlem_gb300.build` (or `__graft_entry__.build()`).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+FL_OK = 0
+FL_ERR_MODEL_NOT_SET = 1
+FL_ERR_PARAMETERS_NOT_SET = 2
+FL_ERR_INVALID_NUM_PARAMETERS = 3
+FL_ERR_BUILDER_SITES_NOT_SET = 4
+FL_ERR_BUILDER_BOUNDS_NOT_SET = 5
+FL_ERR_BUILDER_VORONOI = 6
+FL_ERR_INVALID_ARGUMENT = 20
+FL_ERR_CUDA = 21
+FL_ERR_OUT_OF_MEMORY = 22
+FL_ERR_DEVICE_LIMIT = 23
+
+# Every symbol include/fastlem_gb300.h declares.
+EXPORTS = [
+    "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
+    "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error",
+    "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
+    "fl_probe_rng_f64", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
+]
+
+c_u32, c_u64, c_int, c_dbl, vp = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+P = ctypes.POINTER
+
+
+class FastlemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fastlem_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        raise FastlemError(-1, f"{path} is missing; build it with `python -m fastlem_gb300.build`")
+    L = ctypes.CDLL(path)
+    L.fl_graph_create.argtypes = [c_u32, vp, vp, vp, vp, vp, c_u32, vp, vp, P(vp)]
+    L.fl_graph_destroy.argtypes = [vp]
+    L.fl_graph_destroy.restype = None
+    gen = [vp, c_u32, vp, vp, vp, vp, vp, ctypes.c_int64, vp, P(c_u32)]
+    L.fl_generate.argtypes = gen
+    L.fl_generate_timed.argtypes = gen + [P(c_dbl), P(c_dbl)]
+    L.fl_graph_num_sites.argtypes = [vp]
+    L.fl_graph_num_sites.restype = c_u32
+    L.fl_graph_num_slots.argtypes = [vp]
+    L.fl_graph_num_slots.restype = c_u64
+    L.fl_last_error.restype = ctypes.c_char_p
+    L.fl_probe_receivers.argtypes = [vp, vp, vp, vp, P(c_int)]
+    L.fl_probe_lakes.argtypes = [vp, vp, c_u32, vp, vp, vp]
+    L.fl_probe_tree_pass.argtypes = [vp, vp, c_u32, vp, vp, vp, vp, vp, vp, vp, P(c_int)]
+    L.fl_probe_prim_rank.argtypes = [vp, vp, c_u32, vp]
+    L.fl_probe_rng_f64.argtypes = [c_u64, c_u64, c_u64, vp]
+    L.fl_random_sites.argtypes = [c_u64, c_dbl, c_dbl, c_dbl, c_dbl, c_u64, c_int, vp, vp]
+    L.fl_relax_sites.argtypes = [c_u32, vp, vp, c_dbl, c_dbl, c_dbl, c_dbl, c_u32]
+    L.fl_build_graph.argtypes = [c_u32, vp, vp, c_dbl, c_dbl, c_dbl, c_dbl, vp, vp, vp, c_u64,
+                                 vp, vp, P(c_u64), P(c_u32)]
+    L.fl_triangulate.argtypes = [c_u32, vp, vp, vp, c_u64]
+    L.fl_triangulate.restype = ctypes.c_int64
+    _lib = L
+    return L
+
+
+def last_error():
+    return lib().fl_last_error().decode()
+
+
+def check(rc):
+    if rc != FL_OK:
+        raise FastlemError(rc, last_error())
+    return rc
+
+
+def ptr(a):
+    """Raw pointer of a C-contiguous numpy array (None passes NULL)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(vp)
+
+
+def as_u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def as_f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def as_u8(a):
+    return np.ascontiguousarray(a, dtype=np.uint8)

@@ -1,0 +1,829 @@
+// solver.cu -- GB300 (sm_103a) landscape-evolution solve and its C ABI.
+//
+// One fl_graph = one terrain model resident in HBM (CSR adjacency in the
+// reference's per-row insertion order, cell areas) plus the solver workspace.
+// fl_generate() runs fastlem's fixed-point loop (src/lem/generator.rs:140-210) on the
+// device:
+//   1. receivers      steepest-descent neighbour, first maximum wins (stream_tree.rs:109-137)
+//   2. lakes          only when some non-outlet site has no lower neighbour:
+//                     basin labels by pointer jumping (stream_tree.rs:139-173), then per
+//                     lake the first site processed by the reference's lake heap that
+//                     touches it -- a packed 64-bit atomicMin of (heap rank << 32 | slot)
+//                     -- and the reversal of the receiver path from there to the lake
+//                     bottom (stream_tree.rs:175-243)
+//   3. levels         breadth-first levels of every outlet's basin over donors
+//                     (drainage_basin.rs:13-36)
+//   4. drainage area  bottom-up by level; each site pulls its donors' areas walking
+//                     its adjacency row backwards, which is exactly the addition
+//                     order of the reference's reversed BFS (generator.rs:154-159)
+//   5. response time  top-down by level (generator.rs:162-174)
+//      + elevation    (generator.rs:177-203), `changed` flag
+// All FP64 arithmetic is written with explicit round-to-nearest intrinsics, so no
+// multiply-add is ever contracted and every value is bit-identical to the
+// reference's evaluation order.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fastlem_gb300.h"
+#include "rng.h"
+
+namespace fl {
+bool lake_heap_rank(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
+                    const uint32_t* outlets, uint32_t n_out, uint32_t* rank);
+}
+
+namespace {
+
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr uint64_t kNoKey = ~0ull;
+constexpr double kEpsilon = 2.220446049250313e-16;   // f64::EPSILON
+constexpr int kThreads = 256;
+
+thread_local std::string g_err;
+
+void set_err(const char* what, cudaError_t e) {
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+    g_err = buf;
+}
+
+#define FL_CU(call)                                                               \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            set_err(#call, e_);                                                   \
+            return e_ == cudaErrorMemoryAllocation ? FL_ERR_OUT_OF_MEMORY : FL_ERR_CUDA; \
+        }                                                                         \
+    } while (0)
+
+#define FL_TRY(expr)            \
+    do {                        \
+        int rc_ = (expr);       \
+        if (rc_ != FL_OK) return rc_; \
+    } while (0)
+
+// Device flags (int32 slots of fl_graph::d_flags).
+enum Flag { kHasLake = 0, kChanged = 1, kJumped = 2, kError = 3, kNumFlags = 8 };
+
+inline unsigned blocks_for(uint64_t n, int t = kThreads) {
+    uint64_t b = (n + t - 1) / t;
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(b, 1u << 30));
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// elev[i] = base[i] + gen::<f64>() * f64::EPSILON, sample i of seed_from_u64(0)
+// (generator.rs:134-138).  One thread per ChaCha block = 8 consecutive sites.
+__global__ void k_initial_elevation(uint32_t n, const double* __restrict__ base,
+                                    double* __restrict__ elev) {
+    uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b * 8 >= n) return;
+    uint32_t key[8];
+    fl::key_from_u64(0, key);
+    uint32_t w[16];
+    fl::chacha12_block(key, b, w);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        uint64_t i = b * 8 + m;
+        if (i < n) {
+            uint64_t v = (uint64_t)w[2 * m] | ((uint64_t)w[2 * m + 1] << 32);
+            elev[i] = __dadd_rn(base[i], __dmul_rn(fl::u64_to_unit_f64(v), kEpsilon));
+        }
+    }
+}
+
+__global__ void k_rng_f64(uint64_t seed, uint64_t first, uint64_t count, double* out) {
+    uint64_t m = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= count) return;
+    uint32_t key[8];
+    fl::key_from_u64(seed, key);
+    uint64_t idx = first + m;
+    uint32_t w[16];
+    fl::chacha12_block(key, idx >> 3, w);
+    uint32_t k = (uint32_t)(idx & 7) * 2;
+    out[m] = fl::u64_to_unit_f64((uint64_t)w[k] | ((uint64_t)w[k + 1] << 32));
+}
+
+// Length of edge (i, j) as `graph.has_edge(i, j)` reports it: the first entry of
+// row i with column j, else 1.0 (generator.rs:164-171).
+__device__ __forceinline__ double edge_len_or_one(const uint32_t* __restrict__ row,
+                                                  const uint32_t* __restrict__ col,
+                                                  const double* __restrict__ len, uint32_t i,
+                                                  uint32_t j) {
+    for (uint32_t s = row[i], e = row[i + 1]; s < e; ++s)
+        if (col[s] == j) return len[s];
+    return 1.0;
+}
+
+// Steepest-descent receivers (stream_tree.rs:109-137).  rlen[i] = length of the
+// edge to the receiver (1.0 when next[i] == i).  Flags kHasLake when a non-outlet
+// site keeps itself as receiver.
+__global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
+                            const uint32_t* __restrict__ col, const double* __restrict__ len,
+                            const double* __restrict__ elev, const uint8_t* __restrict__ outlet,
+                            uint32_t* __restrict__ next, double* __restrict__ rlen,
+                            int* __restrict__ flags) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (outlet[i]) {
+        next[i] = i;
+        rlen[i] = 1.0;
+        return;
+    }
+    const double ei = elev[i];
+    double steepest = 0.0;
+    uint32_t best = i, best_slot = kNone;
+    const uint32_t s0 = row[i], s1 = row[i + 1];
+    for (uint32_t s = s0; s < s1; ++s) {
+        uint32_t j = col[s];
+        double ej = elev[j];
+        if (ei > ej) {
+            double slope = __ddiv_rn(__dsub_rn(ei, ej), len[s]);
+            if (slope > steepest) {
+                steepest = slope;
+                best = j;
+                best_slot = s;
+            }
+        }
+    }
+    next[i] = best;
+    if (best_slot == kNone) {
+        rlen[i] = 1.0;
+        flags[kHasLake] = 1;
+    } else {
+        uint32_t s = s0;
+        while (col[s] != best) ++s;   // first occurrence, as has_edge reports it
+        rlen[i] = len[s];
+    }
+}
+
+__global__ void k_copy_u32(uint32_t n, const uint32_t* __restrict__ a, uint32_t* __restrict__ b) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = a[i];
+}
+
+// One pointer-jumping round: lab_out[i] = lab_in[lab_in[i]].  Roots (next[r] == r)
+// are fixed points, so after ceil(log2(depth)) rounds lab[i] is the basin root
+// (stream_tree.rs:139-173, "subroot").
+__global__ void k_jump(uint32_t n, const uint32_t* __restrict__ lab_in,
+                       uint32_t* __restrict__ lab_out, int* __restrict__ flags) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t l = lab_in[i];
+    uint32_t ll = lab_in[l];
+    lab_out[i] = ll;
+    if (ll != l) flags[kJumped] = 1;
+}
+
+__global__ void k_fill_u64(uint32_t n, uint64_t* __restrict__ a, uint64_t v) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+// For every site v the lake heap processes (rank[v] != none) and every neighbour j
+// lying in a lake L other than v's own basin: best[L] = min((rank[v] << 32) | slot).
+// The minimum is the first processed site touching L and, within its row, the
+// first entry in L -- the pair at which the reference flips L (stream_tree.rs:204-230).
+__global__ void k_lake_keys(uint32_t n, const uint32_t* __restrict__ row,
+                            const uint32_t* __restrict__ col, const uint32_t* __restrict__ rank,
+                            const uint32_t* __restrict__ lab, const uint8_t* __restrict__ outlet,
+                            unsigned long long* __restrict__ best) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    uint32_t r = rank[v];
+    if (r == kNone) return;
+    uint32_t lv = lab[v];
+    const uint32_t s0 = row[v], s1 = row[v + 1];
+    for (uint32_t s = s0; s < s1; ++s) {
+        uint32_t L = lab[col[s]];
+        if (outlet[L] || L == lv) continue;
+        unsigned long long key = ((unsigned long long)r << 32) | (unsigned long long)(s - s0);
+        if (key < best[L]) atomicMin(&best[L], key);
+    }
+}
+
+// One thread per lake: reverse the receiver path from j* to the lake bottom and
+// hang it on v* (stream_tree.rs:214-228).  Lakes are disjoint and each flip only
+// touches its own lake's sites, so lakes run independently.
+__global__ void k_lake_flip(uint32_t n, const uint32_t* __restrict__ row,
+                            const uint32_t* __restrict__ col, const double* __restrict__ len,
+                            const unsigned long long* __restrict__ best,
+                            const uint32_t* __restrict__ site_of_rank, uint32_t* next,
+                            double* rlen, int* flags) {
+    uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= n) return;
+    unsigned long long key = best[L];
+    if (key == kNoKey) return;
+    uint32_t v = site_of_rank[key >> 32];
+    uint32_t j = col[row[v] + (uint32_t)(key & 0xffffffffu)];
+    uint32_t k = j, nk = v;
+    for (uint32_t steps = 0;; ++steps) {
+        if (steps > n) {             // a cycle: cannot happen on a descent forest
+            flags[kError] = 1;
+            return;
+        }
+        uint32_t nx = next[k];
+        if (nx == k) break;
+        next[k] = nk;
+        rlen[k] = edge_len_or_one(row, col, len, k, nk);
+        nk = k;
+        k = nx;
+    }
+    next[k] = nk;
+    rlen[k] = edge_len_or_one(row, col, len, k, nk);
+}
+
+// Level 0 of the basin traversal: the outlets, each its own basin.
+__global__ void k_levels_init(uint32_t n_out, const uint32_t* __restrict__ outlets,
+                              uint32_t* __restrict__ order, uint32_t* __restrict__ bas,
+                              uint32_t* __restrict__ lvl_off, uint32_t* __restrict__ tail) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_out) {
+        uint32_t o = outlets[i];
+        order[i] = o;
+        bas[o] = o;
+    }
+    if (i == 0) {
+        lvl_off[0] = 0;
+        lvl_off[1] = n_out;
+        *tail = n_out;
+    }
+}
+
+// Expand level L into level L+1: every donor d of a level-L site v (next[d] == v,
+// drainage_basin.rs:267-271) is appended.  Grid-stride over the level.
+__global__ void k_levels_expand(uint32_t L, const uint32_t* __restrict__ row,
+                                const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
+                                uint32_t* __restrict__ order, uint32_t* __restrict__ bas,
+                                const uint32_t* __restrict__ lvl_off, uint32_t* tail) {
+    uint32_t beg = lvl_off[L], end = lvl_off[L + 1];
+    for (uint32_t idx = beg + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
+         idx += gridDim.x * blockDim.x) {
+        uint32_t v = order[idx];
+        uint32_t b = bas[v];
+        for (uint32_t s = row[v], e = row[v + 1]; s < e; ++s) {
+            uint32_t d = col[s];
+            if (next[d] == v && d != v) {
+                uint32_t pos = atomicAdd(tail, 1u);
+                order[pos] = d;
+                bas[d] = b;
+            }
+        }
+    }
+}
+
+__global__ void k_levels_close(uint32_t L, uint32_t* __restrict__ lvl_off,
+                               const uint32_t* __restrict__ tail) {
+    lvl_off[L + 2] = *tail;
+}
+
+// Drainage area of level-L sites: A_v = a_v + A_{d_m} + ... + A_{d_1}, donors taken
+// in reverse adjacency order (the reference's reversed BFS, generator.rs:154-159).
+__global__ void k_area_level(uint32_t L, const uint32_t* __restrict__ row,
+                             const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
+                             const uint32_t* __restrict__ order, const uint32_t* __restrict__ lvl_off,
+                             const double* __restrict__ area, double* A) {
+    uint32_t beg = lvl_off[L], end = lvl_off[L + 1];
+    for (uint32_t idx = beg + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
+         idx += gridDim.x * blockDim.x) {
+        uint32_t v = order[idx];
+        double a = area[v];
+        for (uint32_t s = row[v + 1]; s-- > row[v];) {
+            uint32_t d = col[s];
+            if (next[d] == v && d != v) a = __dadd_rn(a, A[d]);
+        }
+        A[v] = a;
+    }
+}
+
+// Response time and elevation of level-L sites (generator.rs:162-203):
+//   t_v = 0 + (t_next + (1 / (k_v * sqrt(A_v))) * len)      (outlet: t_next = 0, len = 1)
+//   e_v = e_o + u_v * max(t_v - t_o, 0), then the optional slope clamp against the
+//   receiver's already-updated elevation.
+__global__ void k_time_elev_level(uint32_t L, const uint32_t* __restrict__ next,
+                                  const uint32_t* __restrict__ order,
+                                  const uint32_t* __restrict__ lvl_off,
+                                  const uint32_t* __restrict__ bas, const double* __restrict__ A,
+                                  const double* __restrict__ rlen, const double* __restrict__ kk,
+                                  const double* __restrict__ uu, const double* __restrict__ tanms,
+                                  double* t, double* elev, int* flags) {
+    uint32_t beg = lvl_off[L], end = lvl_off[L + 1];
+    for (uint32_t idx = beg + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
+         idx += gridDim.x * blockDim.x) {
+        uint32_t v = order[idx];
+        uint32_t j = next[v];
+        double dist = rlen[v];
+        double tj = (j == v) ? 0.0 : t[j];
+        double cel = __dmul_rn(kk[v], __dsqrt_rn(A[v]));
+        double tv = __dadd_rn(0.0, __dadd_rn(tj, __dmul_rn(__ddiv_rn(1.0, cel), dist)));
+        t[v] = tv;
+        uint32_t o = bas[v];
+        double to = (o == v) ? tv : t[o];
+        double dt = __dsub_rn(tv, to);
+        double old_e = elev[v];
+        double ne = __dadd_rn(elev[o], __dmul_rn(uu[v], dt > 0.0 ? dt : 0.0));
+        double tn = tanms[v];
+        if (!isnan(tn)) {
+            double ej = (j == v) ? old_e : elev[j];
+            double slope = __ddiv_rn(__dsub_rn(ne, ej), dist);
+            if (slope > tn) ne = __dadd_rn(ej, __dmul_rn(tn, dist));
+        }
+        if (ne != old_e) flags[kChanged] = 1;
+        elev[v] = ne;
+    }
+}
+
+__global__ void k_fill_f64(uint32_t n, double* __restrict__ a, const double* __restrict__ src) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = src ? src[i] : 0.0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Model handle
+// ---------------------------------------------------------------------------
+struct fl_graph {
+    uint32_t n = 0;
+    uint64_t nnz = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // host copies used by the host-side lake-heap rank
+    std::vector<uint32_t> h_row, h_col;
+    std::vector<double> h_len;
+    std::vector<uint32_t> def_outlets;
+    // cached rank for one outlet list
+    std::vector<uint32_t> rank_key;
+    bool rank_valid = false;
+    bool rank_uploaded = false;
+    std::vector<uint32_t> h_rank;
+    // device arrays
+    uint32_t *d_row = nullptr, *d_col = nullptr;
+    double *d_len = nullptr, *d_area = nullptr;
+    double *d_k = nullptr, *d_u = nullptr, *d_tan = nullptr, *d_elev = nullptr, *d_A = nullptr,
+           *d_t = nullptr, *d_rlen = nullptr, *d_base = nullptr;
+    uint32_t *d_next = nullptr, *d_lab = nullptr, *d_lab2 = nullptr, *d_rank = nullptr,
+             *d_sor = nullptr, *d_bas = nullptr, *d_order = nullptr, *d_lvl = nullptr,
+             *d_outlets = nullptr, *d_tail = nullptr;
+    uint8_t* d_outlet = nullptr;
+    unsigned long long* d_best = nullptr;
+    int* d_flags = nullptr;
+    uint32_t lvl_cap = 0;
+};
+
+namespace {
+
+template <class T>
+int dalloc(T** p, uint64_t count) {
+    FL_CU(cudaMalloc((void**)p, std::max<uint64_t>(1, count) * sizeof(T)));
+    return FL_OK;
+}
+
+void free_graph(fl_graph* g) {
+    if (!g) return;
+    void* ptrs[] = {g->d_row, g->d_col, g->d_len, g->d_area, g->d_k, g->d_u, g->d_tan, g->d_elev,
+                    g->d_A, g->d_t, g->d_rlen, g->d_base, g->d_next, g->d_lab, g->d_lab2,
+                    g->d_rank, g->d_sor, g->d_bas, g->d_order, g->d_lvl, g->d_outlets,
+                    g->d_tail, g->d_outlet, g->d_best, g->d_flags};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+int alloc_workspace(fl_graph* g) {
+    uint32_t n = g->n;
+    FL_TRY(dalloc(&g->d_k, n));
+    FL_TRY(dalloc(&g->d_u, n));
+    FL_TRY(dalloc(&g->d_tan, n));
+    FL_TRY(dalloc(&g->d_elev, n));
+    FL_TRY(dalloc(&g->d_A, n));
+    FL_TRY(dalloc(&g->d_t, n));
+    FL_TRY(dalloc(&g->d_rlen, n));
+    FL_TRY(dalloc(&g->d_base, n));
+    FL_TRY(dalloc(&g->d_next, n));
+    FL_TRY(dalloc(&g->d_lab, n));
+    FL_TRY(dalloc(&g->d_lab2, n));
+    FL_TRY(dalloc(&g->d_rank, n));
+    FL_TRY(dalloc(&g->d_sor, n));
+    FL_TRY(dalloc(&g->d_bas, n));
+    FL_TRY(dalloc(&g->d_order, n));
+    FL_TRY(dalloc(&g->d_outlets, n));
+    FL_TRY(dalloc(&g->d_tail, 1));
+    FL_TRY(dalloc(&g->d_outlet, n));
+    FL_TRY(dalloc(&g->d_best, n));
+    FL_TRY(dalloc(&g->d_flags, kNumFlags));
+    g->lvl_cap = n + 2;
+    FL_TRY(dalloc(&g->d_lvl, g->lvl_cap));
+    return FL_OK;
+}
+
+int read_flags(fl_graph* g, int* h) {
+    FL_CU(cudaMemcpyAsync(h, g->d_flags, kNumFlags * sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
+    return FL_OK;
+}
+
+int clear_flags(fl_graph* g) {
+    FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
+    return FL_OK;
+}
+
+// Outlet list as generate() resolves it (generator.rs:120-132).
+std::vector<uint32_t> resolve_outlets(const fl_graph* g, const uint8_t* is_outlet) {
+    std::vector<uint32_t> o;
+    for (uint32_t i = 0; i < g->n; ++i)
+        if (is_outlet[i]) o.push_back(i);
+    if (o.empty()) o = g->def_outlets;
+    return o;
+}
+
+// Uploads the outlet list and table, computing (or reusing) the lake-heap rank.
+int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_rank) {
+    uint32_t n = g->n;
+    std::vector<uint8_t> table(n, 0);
+    for (uint32_t o : outlets) table[o] = 1;
+    FL_CU(cudaMemcpyAsync(g->d_outlet, table.data(), n, cudaMemcpyHostToDevice, g->stream));
+    if (!outlets.empty())
+        FL_CU(cudaMemcpyAsync(g->d_outlets, outlets.data(), outlets.size() * 4,
+                              cudaMemcpyHostToDevice, g->stream));
+    if (!g->rank_valid || g->rank_key != outlets) {
+        g->rank_valid = false;
+        g->rank_uploaded = false;
+        g->rank_key = outlets;
+    }
+    if (need_rank && !g->rank_uploaded) {
+        if (!g->rank_valid) {
+            g->h_rank.resize(n);
+            if (!fl::lake_heap_rank(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
+                                    outlets.data(), (uint32_t)outlets.size(), g->h_rank.data())) {
+                g_err = "NaN edge length in the lake traversal";
+                return FL_ERR_INVALID_ARGUMENT;
+            }
+            g->rank_valid = true;
+        }
+        std::vector<uint32_t> sor(n, kNone);
+        for (uint32_t v = 0; v < n; ++v)
+            if (g->h_rank[v] != kNone) sor[g->h_rank[v]] = v;
+        FL_CU(cudaMemcpyAsync(g->d_rank, g->h_rank.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
+        FL_CU(cudaMemcpyAsync(g->d_sor, sor.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
+        FL_CU(cudaStreamSynchronize(g->stream));
+        g->rank_uploaded = true;
+    }
+    return FL_OK;
+}
+
+// Receivers for the current elevations.  Returns has_lake in *has_lake.
+int run_receivers(fl_graph* g, int* has_lake) {
+    FL_TRY(clear_flags(g));
+    k_receivers<<<blocks_for(g->n), kThreads, 0, g->stream>>>(g->n, g->d_row, g->d_col, g->d_len,
+                                                                g->d_elev, g->d_outlet, g->d_next,
+                                                                g->d_rlen, g->d_flags);
+    FL_CU(cudaGetLastError());
+    int h[kNumFlags];
+    FL_TRY(read_flags(g, h));
+    *has_lake = h[kHasLake];
+    return FL_OK;
+}
+
+// Basin labels of d_next into d_lab.
+int run_labels(fl_graph* g) {
+    uint32_t n = g->n;
+    k_copy_u32<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_next, g->d_lab);
+    FL_CU(cudaGetLastError());
+    for (int round = 0;; ++round) {
+        if (round > 64) {
+            g_err = "basin labelling did not converge";
+            return FL_ERR_DEVICE_LIMIT;
+        }
+        FL_TRY(clear_flags(g));
+        k_jump<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_lab, g->d_lab2, g->d_flags);
+        FL_CU(cudaGetLastError());
+        std::swap(g->d_lab, g->d_lab2);
+        int h[kNumFlags];
+        FL_TRY(read_flags(g, h));
+        if (!h[kJumped]) break;
+    }
+    return FL_OK;
+}
+
+// Lake re-routing on d_next (labels must be current).
+int run_lakes(fl_graph* g) {
+    uint32_t n = g->n;
+    FL_TRY(clear_flags(g));
+    k_fill_u64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, (uint64_t*)g->d_best, kNoKey);
+    k_lake_keys<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_row, g->d_col, g->d_rank,
+                                                             g->d_lab, g->d_outlet, g->d_best);
+    k_lake_flip<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_row, g->d_col, g->d_len,
+                                                             g->d_best, g->d_sor, g->d_next,
+                                                             g->d_rlen, g->d_flags);
+    FL_CU(cudaGetLastError());
+    int h[kNumFlags];
+    FL_TRY(read_flags(g, h));
+    if (h[kError]) {
+        g_err = "lake re-routing walked a cycle";
+        return FL_ERR_DEVICE_LIMIT;
+    }
+    return FL_OK;
+}
+
+constexpr uint32_t kLevelBatch = 64;
+
+// Basin levels from the outlets; returns the number of non-empty levels.
+int run_levels(fl_graph* g, uint32_t n_out, uint32_t* n_levels) {
+    unsigned grid = 152 * 4;
+    k_levels_init<<<blocks_for(n_out), kThreads, 0, g->stream>>>(n_out, g->d_outlets, g->d_order,
+                                                                   g->d_bas, g->d_lvl, g->d_tail);
+    FL_CU(cudaGetLastError());
+    uint32_t L = 0;
+    while (true) {
+        for (uint32_t b = 0; b < kLevelBatch; ++b, ++L) {
+            if (L + 2 >= g->lvl_cap) {
+                g_err = "basin depth exceeds the site count";
+                return FL_ERR_DEVICE_LIMIT;
+            }
+            k_levels_expand<<<grid, kThreads, 0, g->stream>>>(L, g->d_row, g->d_col, g->d_next,
+                                                                g->d_order, g->d_bas, g->d_lvl,
+                                                                g->d_tail);
+            k_levels_close<<<1, 1, 0, g->stream>>>(L, g->d_lvl, g->d_tail);
+        }
+        FL_CU(cudaGetLastError());
+        // offsets of the last two levels written: lvl[L] .. lvl[L+1]
+        uint32_t off[2];
+        FL_CU(cudaMemcpyAsync(off, g->d_lvl + L, 8, cudaMemcpyDeviceToHost, g->stream));
+        FL_CU(cudaStreamSynchronize(g->stream));
+        if (off[1] == off[0]) break;   // level L is empty
+    }
+    // count non-empty levels
+    std::vector<uint32_t> off(L + 2);
+    FL_CU(cudaMemcpyAsync(off.data(), g->d_lvl, (L + 2) * 4ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
+    uint32_t nl = 0;
+    while (nl < L + 1 && off[nl + 1] > off[nl]) ++nl;
+    *n_levels = nl;
+    return FL_OK;
+}
+
+// Drainage areas, response times, elevations on final receivers.
+int run_tree_pass(fl_graph* g, uint32_t n_out, int* changed) {
+    uint32_t nl = 0;
+    FL_TRY(run_levels(g, n_out, &nl));
+    unsigned grid = 152 * 4;
+    for (uint32_t L = nl; L-- > 0;)
+        k_area_level<<<grid, kThreads, 0, g->stream>>>(L, g->d_row, g->d_col, g->d_next, g->d_order,
+                                                        g->d_lvl, g->d_area, g->d_A);
+    FL_CU(cudaGetLastError());
+    FL_TRY(clear_flags(g));
+    for (uint32_t L = 0; L < nl; ++L)
+        k_time_elev_level<<<grid, kThreads, 0, g->stream>>>(L, g->d_next, g->d_order, g->d_lvl,
+                                                             g->d_bas, g->d_A, g->d_rlen, g->d_k,
+                                                             g->d_u, g->d_tan, g->d_t, g->d_elev,
+                                                             g->d_flags);
+    FL_CU(cudaGetLastError());
+    int h[kNumFlags];
+    FL_TRY(read_flags(g, h));
+    *changed = h[kChanged];
+    return FL_OK;
+}
+
+int upload_params(fl_graph* g, const double* base, const double* k, const double* u,
+                  const double* max_slope) {
+    uint32_t n = g->n;
+    std::vector<double> tanv(n);
+    for (uint32_t i = 0; i < n; ++i)
+        tanv[i] = (max_slope && !std::isnan(max_slope[i])) ? std::tan(max_slope[i]) : NAN;
+    if (base) FL_CU(cudaMemcpyAsync(g->d_base, base, n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    if (k) FL_CU(cudaMemcpyAsync(g->d_k, k, n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    if (u) FL_CU(cudaMemcpyAsync(g->d_u, u, n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    FL_CU(cudaMemcpyAsync(g->d_tan, tanv.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
+    return FL_OK;
+}
+
+int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const double* k,
+                  const double* u, const uint8_t* is_outlet, const double* max_slope,
+                  int64_t max_iter, double* out_elev, uint32_t* out_iters, double* loop_ms,
+                  double* total_ms) {
+    g_err.clear();
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    if (!base || !k || !u || !is_outlet) return FL_ERR_PARAMETERS_NOT_SET;
+    if (n_params != g->n) return FL_ERR_INVALID_NUM_PARAMETERS;
+    if (!out_elev) return FL_ERR_INVALID_ARGUMENT;
+    auto t_start = std::chrono::steady_clock::now();
+    uint32_t n = g->n;
+    std::vector<uint32_t> outlets = resolve_outlets(g, is_outlet);
+    FL_TRY(upload_params(g, base, k, u, max_slope));
+    FL_TRY(set_outlets(g, outlets, false));
+    k_initial_elevation<<<blocks_for((n + 7) / 8), kThreads, 0, g->stream>>>(n, g->d_base, g->d_elev);
+    FL_CU(cudaGetLastError());
+    FL_CU(cudaEventRecord(g->ev0, g->stream));
+    if (max_iter > 0xffffffffll) max_iter = 0xffffffffll;
+    uint64_t limit = max_iter < 0 ? 0xffffffffull : (uint64_t)max_iter;
+    uint32_t iters = 0;
+    for (uint64_t it = 0; it < limit; ++it) {
+        ++iters;
+        int has_lake = 0, changed = 0;
+        FL_TRY(run_receivers(g, &has_lake));
+        if (has_lake) {
+            FL_TRY(set_outlets(g, outlets, true));
+            FL_TRY(run_labels(g));
+            FL_TRY(run_lakes(g));
+        }
+        FL_TRY(run_tree_pass(g, (uint32_t)outlets.size(), &changed));
+        if (!changed) break;
+    }
+    FL_CU(cudaEventRecord(g->ev1, g->stream));
+    FL_CU(cudaMemcpyAsync(out_elev, g->d_elev, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
+    if (out_iters) *out_iters = iters;
+    if (loop_ms) {
+        float ms = 0;
+        FL_CU(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+        *loop_ms = ms;
+    }
+    if (total_ms)
+        *total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    return FL_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* fl_last_error(void) { return g_err.c_str(); }
+
+int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
+                    const double* area, const uint32_t* default_outlets, uint32_t n_default,
+                    const double* xs, const double* ys, fl_graph** out) {
+    (void)xs;
+    (void)ys;
+    g_err.clear();
+    if (!out || !row_ptr || (!col && n) || !area || (n_default && !default_outlets) || n == 0 ||
+        n >= kNone) {
+        g_err = "invalid graph arguments";
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    uint64_t nnz = row_ptr[n];
+    if (row_ptr[0] != 0) { g_err = "row_ptr[0] != 0"; return FL_ERR_INVALID_ARGUMENT; }
+    for (uint32_t i = 0; i < n; ++i)
+        if (row_ptr[i + 1] < row_ptr[i]) { g_err = "row_ptr not monotone"; return FL_ERR_INVALID_ARGUMENT; }
+    for (uint64_t s = 0; s < nnz; ++s)
+        if (col[s] >= n || std::isnan(len[s])) { g_err = "column out of range or NaN length"; return FL_ERR_INVALID_ARGUMENT; }
+    for (uint32_t i = 0; i < n_default; ++i)
+        if (default_outlets[i] >= n) { g_err = "default outlet out of range"; return FL_ERR_INVALID_ARGUMENT; }
+    fl_graph* g = new fl_graph();
+    g->n = n;
+    g->nnz = nnz;
+    g->h_row.assign(row_ptr, row_ptr + n + 1);
+    g->h_col.assign(col, col + nnz);
+    g->h_len.assign(len, len + nnz);
+    g->def_outlets.assign(default_outlets, default_outlets + n_default);
+    int rc = FL_OK;
+    auto fail = [&](int r) { free_graph(g); return r; };
+    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { set_err("cudaStreamCreate", e); return fail(FL_ERR_CUDA); }
+    if (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess) {
+        g_err = "cudaEventCreate failed";
+        return fail(FL_ERR_CUDA);
+    }
+    if ((rc = dalloc(&g->d_row, n + 1)) || (rc = dalloc(&g->d_col, nnz)) ||
+        (rc = dalloc(&g->d_len, nnz)) || (rc = dalloc(&g->d_area, n)) || (rc = alloc_workspace(g)))
+        return fail(rc);
+    if (cudaMemcpy(g->d_row, row_ptr, (n + 1) * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (nnz && cudaMemcpy(g->d_col, col, nnz * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        (nnz && cudaMemcpy(g->d_len, len, nnz * 8ull, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        cudaMemcpy(g->d_area, area, n * 8ull, cudaMemcpyHostToDevice) != cudaSuccess) {
+        g_err = "graph upload failed";
+        return fail(FL_ERR_CUDA);
+    }
+    *out = g;
+    return FL_OK;
+}
+
+void fl_graph_destroy(fl_graph* g) { free_graph(g); }
+
+uint32_t fl_graph_num_sites(const fl_graph* g) { return g ? g->n : 0; }
+uint64_t fl_graph_num_slots(const fl_graph* g) { return g ? g->nnz : 0; }
+
+int fl_generate(fl_graph* g, uint32_t n_params, const double* base, const double* erodibility,
+                const double* uplift, const uint8_t* is_outlet, const double* max_slope,
+                int64_t max_iteration, double* out_elev, uint32_t* out_iterations) {
+    return generate_impl(g, n_params, base, erodibility, uplift, is_outlet, max_slope,
+                         max_iteration, out_elev, out_iterations, nullptr, nullptr);
+}
+
+int fl_generate_timed(fl_graph* g, uint32_t n_params, const double* base,
+                      const double* erodibility, const double* uplift, const uint8_t* is_outlet,
+                      const double* max_slope, int64_t max_iteration, double* out_elev,
+                      uint32_t* out_iterations, double* loop_ms, double* total_ms) {
+    return generate_impl(g, n_params, base, erodibility, uplift, is_outlet, max_slope,
+                         max_iteration, out_elev, out_iterations, loop_ms, total_ms);
+}
+
+int fl_probe_receivers(fl_graph* g, const double* elev, const uint8_t* outlet_table,
+                       uint32_t* next_out, int* has_lake) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    uint32_t n = g->n;
+    FL_CU(cudaMemcpyAsync(g->d_elev, elev, n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    FL_CU(cudaMemcpyAsync(g->d_outlet, outlet_table, n, cudaMemcpyHostToDevice, g->stream));
+    int hl = 0;
+    FL_TRY(run_receivers(g, &hl));
+    FL_CU(cudaMemcpyAsync(next_out, g->d_next, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
+    if (has_lake) *has_lake = hl;
+    return FL_OK;
+}
+
+int fl_probe_lakes(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
+                   const uint32_t* next_in, uint32_t* next_out, uint32_t* label_out) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    uint32_t n = g->n;
+    std::vector<uint32_t> o(outlets, outlets + n_outlets);
+    FL_TRY(set_outlets(g, o, true));
+    FL_CU(cudaMemcpyAsync(g->d_next, next_in, n * 4ull, cudaMemcpyHostToDevice, g->stream));
+    std::vector<double> ones(n, 1.0);
+    FL_CU(cudaMemcpyAsync(g->d_rlen, ones.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    FL_TRY(run_labels(g));
+    if (label_out) {
+        FL_CU(cudaMemcpyAsync(label_out, g->d_lab, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
+    }
+    FL_TRY(run_lakes(g));
+    FL_CU(cudaMemcpyAsync(next_out, g->d_next, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
+    return FL_OK;
+}
+
+int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
+                       const uint32_t* next, const double* erodibility, const double* uplift,
+                       const double* max_slope, double* elev, double* drainage_out,
+                       double* response_out, int* changed) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    uint32_t n = g->n;
+    std::vector<uint32_t> o(outlets, outlets + n_outlets);
+    FL_TRY(upload_params(g, nullptr, erodibility, uplift, max_slope));
+    FL_TRY(set_outlets(g, o, false));
+    FL_CU(cudaMemcpyAsync(g->d_next, next, n * 4ull, cudaMemcpyHostToDevice, g->stream));
+    FL_CU(cudaMemcpyAsync(g->d_elev, elev, n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    // receiver lengths as has_edge reports them
+    std::vector<double> rl(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        rl[i] = 1.0;
+        if (next[i] != i)
+            for (uint32_t s = g->h_row[i]; s < g->h_row[i + 1]; ++s)
+                if (g->h_col[s] == next[i]) { rl[i] = g->h_len[s]; break; }
+    }
+    FL_CU(cudaMemcpyAsync(g->d_rlen, rl.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    k_fill_f64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_A, g->d_area);
+    k_fill_f64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_t, nullptr);
+    int ch = 0;
+    FL_TRY(run_tree_pass(g, n_outlets, &ch));
+    FL_CU(cudaMemcpyAsync(elev, g->d_elev, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    if (drainage_out) FL_CU(cudaMemcpyAsync(drainage_out, g->d_A, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    if (response_out) FL_CU(cudaMemcpyAsync(response_out, g->d_t, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
+    if (changed) *changed = ch;
+    return FL_OK;
+}
+
+int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets, uint32_t* rank) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    if (!fl::lake_heap_rank(g->n, g->h_row.data(), g->h_col.data(), g->h_len.data(), outlets,
+                            n_outlets, rank)) {
+        g_err = "NaN edge length in the lake traversal";
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    return FL_OK;
+}
+
+int fl_probe_rng_f64(uint64_t seed, uint64_t first, uint64_t count, double* out) {
+    double* d = nullptr;
+    FL_CU(cudaMalloc(&d, std::max<uint64_t>(1, count) * 8));
+    k_rng_f64<<<blocks_for(count), kThreads>>>(seed, first, count, d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, count * 8, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        set_err("fl_probe_rng_f64", e);
+        return FL_ERR_CUDA;
+    }
+    return FL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,156 @@
+/* fastlem_gb300.h -- C ABI of the GB300 landscape-evolution solve.
+ *
+ * The drop-in boundary for fastlem's `TerrainGenerator::generate()`.  A Rust crate
+ * (or any FFI caller) keeps fastlem's public types and forwards to these calls;
+ * no torch or CUDA types appear in any signature.  All arrays are host pointers.
+ *
+ * Status codes (int return values):
+ *   FL_OK                          0
+ *   FL_ERR_MODEL_NOT_SET           1  GenerationError::ModelNotSet            (lem/generator.rs:25)
+ *   FL_ERR_PARAMETERS_NOT_SET      2  GenerationError::ParametersNotSet       (lem/generator.rs:23)
+ *   FL_ERR_INVALID_NUM_PARAMETERS  3  GenerationError::InvalidNumberOfParameters (lem/generator.rs:21)
+ *   FL_ERR_BUILDER_SITES_NOT_SET   4  ModelBuilderError::SitesNotSet          (models/surface/builder.rs:16)
+ *   FL_ERR_BUILDER_BOUNDS_NOT_SET  5  ModelBuilderError::BoundsNotSet         (models/surface/builder.rs:18)
+ *   FL_ERR_BUILDER_VORONOI         6  ModelBuilderError::VoronoiError         (models/surface/builder.rs:20)
+ *   FL_ERR_INVALID_ARGUMENT       20  malformed graph (index out of range, NaN length, size limits)
+ *   FL_ERR_CUDA                   21  a CUDA runtime call failed (message via fl_last_error)
+ *   FL_ERR_OUT_OF_MEMORY          22  device allocation failed
+ *   FL_ERR_DEVICE_LIMIT           23  a device-side loop hit its iteration cap (a graph whose
+ *                                     receiver structure is not a forest; never expected)
+ */
+#ifndef FASTLEM_GB300_H
+#define FASTLEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FL_OK 0
+#define FL_ERR_MODEL_NOT_SET 1
+#define FL_ERR_PARAMETERS_NOT_SET 2
+#define FL_ERR_INVALID_NUM_PARAMETERS 3
+#define FL_ERR_BUILDER_SITES_NOT_SET 4
+#define FL_ERR_BUILDER_BOUNDS_NOT_SET 5
+#define FL_ERR_BUILDER_VORONOI 6
+#define FL_ERR_INVALID_ARGUMENT 20
+#define FL_ERR_CUDA 21
+#define FL_ERR_OUT_OF_MEMORY 22
+#define FL_ERR_DEVICE_LIMIT 23
+
+/* Opaque handle: one terrain model (graph, cell areas, default outlets) resident on
+ * the current CUDA device, with the solver's device workspace. */
+typedef struct fl_graph fl_graph;
+
+/* Upload a model once.  Replaces `TerrainModel2D` as seen through the `Model`
+ * trait (core/traits.rs:12-19, models/surface/model.rs:41-60):
+ *   n                 = model.num()                     (graph.order())
+ *   row_ptr[n+1], col[row_ptr[n]], len[row_ptr[n]]
+ *                     = model.graph(): row i lists graph.neighbors_of(i) in
+ *                       insertion order, col = neighbour, len = edge attribute
+ *   area[n]           = model.areas()
+ *   default_outlets   = model.default_outlets()
+ * xs/ys (optional, may be NULL) are the site coordinates; they only steer the
+ * device-side memory order and never change results.
+ * Returns FL_OK and *out, or an error code. */
+int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
+                    const double* area, const uint32_t* default_outlets, uint32_t n_default,
+                    const double* xs, const double* ys, fl_graph** out);
+
+/* Release a model and its device memory.  NULL is ignored. */
+void fl_graph_destroy(fl_graph* g);
+
+/* `TerrainGenerator::generate()` (lem/generator.rs:90-213) on model `g`.
+ *   g == NULL                                  -> FL_ERR_MODEL_NOT_SET
+ *   base/erodibility/uplift/is_outlet == NULL  -> FL_ERR_PARAMETERS_NOT_SET
+ *   n_params != n                              -> FL_ERR_INVALID_NUM_PARAMETERS
+ * The per-site parameter arrays are `TopographicalParameters` (core/parameters.rs:24-35)
+ * as structure-of-arrays:
+ *   base[i]        base_elevation
+ *   erodibility[i] erodibility
+ *   uplift[i]      uplift_rate
+ *   is_outlet[i]   0 / 1
+ *   max_slope[i]   radians; NaN means None.  max_slope == NULL means None everywhere.
+ * max_iteration: negative means unset (`set_max_iteration` never called: the loop
+ *                bound is u32::MAX); 0 .. u32::MAX as `set_max_iteration(m)` (0 runs no
+ *                iteration and returns the initial elevations).
+ * Outputs: out_elev[n] = Terrain2D::elevations() (models/surface/terrain.rs:31-33),
+ *          *out_iterations = loop bodies executed (may be NULL). */
+int fl_generate(fl_graph* g, uint32_t n_params, const double* base, const double* erodibility,
+                const double* uplift, const uint8_t* is_outlet, const double* max_slope,
+                int64_t max_iteration, double* out_elev, uint32_t* out_iterations);
+
+/* Device-timed variant for benchmarks: same contract as fl_generate, and writes the
+ * device time of the iteration loop (milliseconds, CUDA events on the solver's
+ * stream) and of the whole call including host<->device copies. */
+int fl_generate_timed(fl_graph* g, uint32_t n_params, const double* base,
+                      const double* erodibility, const double* uplift, const uint8_t* is_outlet,
+                      const double* max_slope, int64_t max_iteration, double* out_elev,
+                      uint32_t* out_iterations, double* loop_ms, double* total_ms);
+
+/* Number of vertices / adjacency slots of a model. */
+uint32_t fl_graph_num_sites(const fl_graph* g);
+uint64_t fl_graph_num_slots(const fl_graph* g);
+
+/* Message for the last error on this thread ("" when none). */
+const char* fl_last_error(void);
+
+/* ---- parity probes: one solver stage on host arrays (tests only) ---------------- */
+
+/* Steepest-descent receivers (lem/stream_tree.rs:109-137); outlet_table[i] != 0 keeps
+ * next[i] = i.  Returns FL_OK; *has_lake = 1 when a non-outlet site has no lower
+ * neighbour (lem/stream_tree.rs:139-173). */
+int fl_probe_receivers(fl_graph* g, const double* elev, const uint8_t* outlet_table,
+                       uint32_t* next_out, int* has_lake);
+
+/* Lake re-routing (lem/stream_tree.rs:175-243) of receivers `next_in` for the outlet
+ * list `outlets` (order as generate() resolves it).  Writes the final receivers and
+ * the basin label (root site) of every site before re-routing. */
+int fl_probe_lakes(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
+                   const uint32_t* next_in, uint32_t* next_out, uint32_t* label_out);
+
+/* One drainage-area / response-time / elevation pass (lem/generator.rs:144-203) on
+ * final receivers `next`; elev is updated in place; returns *changed. */
+int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
+                       const uint32_t* next, const double* erodibility, const double* uplift,
+                       const double* max_slope, double* elev, double* drainage_out,
+                       double* response_out, int* changed);
+
+/* The order in which the reference's lake heap processes sites
+ * (lem/stream_tree.rs:184-240), computed on the host: rank[v], UINT32_MAX if never. */
+int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets, uint32_t* rank);
+
+/* `count` samples of StdRng::seed_from_u64(seed).gen::<f64>() drawn on the device,
+ * starting at sample `first` (the initial-elevation noise of lem/generator.rs:134-138). */
+int fl_probe_rng_f64(uint64_t seed, uint64_t first, uint64_t count, double* out);
+
+/* ---- host model builder (models/surface/builder.rs) ------------------------------ */
+
+/* `from_random_sites` sampler (builder.rs:38-52): x = gen_range(x0..x1), then
+ * y = gen_range(y0..y1), per site.  zero_seed != 0 uses StdRng::from_seed([0; 32]) as
+ * fastlem does; otherwise StdRng::seed_from_u64(seed). */
+int fl_random_sites(uint64_t n, double x0, double y0, double x1, double y1, uint64_t seed,
+                    int zero_seed, double* xs, double* ys);
+
+/* `relaxate_sites(times)` (builder.rs:155-200): Lloyd relaxation in place. */
+int fl_relax_sites(uint32_t n, double* xs, double* ys, double x0, double y0, double x1, double y1,
+                   uint32_t times);
+
+/* `build()` (builder.rs:202-281): Delaunay graph (a<b edge rule), clipped Voronoi
+ * areas and hull outlets.  col/len hold `cap` slots (6n suffices); hull holds n. */
+int fl_build_graph(uint32_t n, const double* xs, const double* ys, double x0, double y0,
+                   double x1, double y1, uint32_t* row_ptr, uint32_t* col, double* len,
+                   uint64_t cap, double* area, uint32_t* hull, uint64_t* out_nnz,
+                   uint32_t* out_nhull);
+
+/* Raw triangulation (counter-clockwise triangles); returns the triangle count. */
+int64_t fl_triangulate(uint32_t n, const double* xs, const double* ys, uint32_t* tri,
+                       uint64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTLEM_GB300_H */

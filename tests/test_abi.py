@@ -1,0 +1,72 @@
+"""CPU tests of the C-ABI library: it builds, loads without a GPU, exports every
+symbol include/fastlem_gb300.h declares, and reports fastlem's errors in
+fastlem's order before touching the device."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fastlem_gb300 import (GenerationError, ParameterArrays, TerrainGenerator,
+                           TopographicalParameters)
+from fastlem_gb300 import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "fastlem_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fl_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_the_exported_list():
+    assert declared_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(fl_lib):
+    for name in declared_functions():
+        assert hasattr(fl_lib, name), name
+
+
+def test_status_codes_match_header():
+    src = open(HEADER).read()
+    for name, val in re.findall(r"#define (FL_[A-Z_]+) (\d+)", src):
+        assert getattr(_lib, name) == int(val), name
+
+
+def test_generate_errors_in_reference_order(fl_lib):
+    # ModelNotSet comes first (generator.rs:91-97), whatever else is missing
+    z = np.zeros(4)
+    assert fl_lib.fl_generate(None, 4, None, None, None, None, None, -1, None, None) == 1
+    with pytest.raises(GenerationError) as e:
+        TerrainGenerator.default().generate()
+    assert e.value.kind == "ModelNotSet"
+
+    class FakeModel:
+        def num(self):
+            return 4
+
+    with pytest.raises(GenerationError) as e:
+        TerrainGenerator.default().set_model(FakeModel()).generate()
+    assert e.value.kind == "ParametersNotSet"
+    with pytest.raises(GenerationError) as e:
+        (TerrainGenerator.default().set_model(FakeModel())
+         .set_parameters([TopographicalParameters()] * 3).generate())
+    assert e.value.kind == "InvalidNumberOfParameters"
+    with pytest.raises(GenerationError) as e:
+        TerrainGenerator.default().set_model(FakeModel()).set_parameters(ParameterArrays(5)).generate()
+    assert e.value.kind == "InvalidNumberOfParameters"
+
+
+def test_parameter_defaults_and_setters():
+    p = TopographicalParameters()
+    assert (p.base_elevation, p.erodibility, p.uplift_rate, p.is_outlet, p.max_slope) == \
+        (0.0, 1.0, 1.0, False, None)
+    q = p.set_erodibility(2.0).set_is_outlet(True).set_max_slope(0.3)
+    assert (q.erodibility, q.is_outlet, q.max_slope) == (2.0, True, 0.3)
+    arr = ParameterArrays.from_list([p, q])
+    assert arr.is_outlet.tolist() == [0, 1]
+    assert np.isnan(arr.max_slope[0]) and arr.max_slope[1] == 0.3
