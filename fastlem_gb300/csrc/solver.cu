@@ -74,6 +74,9 @@ void set_err(const char* what, cudaError_t e) {
 // Device flags (int32 slots of fl_graph::d_flags).
 enum Flag { kHasLake = 0, kChanged = 1, kJumped = 2, kError = 3, kNumFlags = 8 };
 
+// Basin levels are expanded this many at a time between host checks.
+constexpr uint32_t kLevelBatch = 64;
+
 inline unsigned blocks_for(uint64_t n, int t = kThreads) {
     uint64_t b = (n + t - 1) / t;
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(b, 1u << 30));
@@ -263,10 +266,11 @@ __global__ void k_levels_init(uint32_t n_out, const uint32_t* __restrict__ outle
 
 // Expand level L into level L+1: every donor d of a level-L site v (next[d] == v,
 // drainage_basin.rs:267-271) is appended.  Grid-stride over the level.
-__global__ void k_levels_expand(uint32_t L, const uint32_t* __restrict__ row,
+__global__ void k_levels_expand(uint32_t L, uint32_t cap, const uint32_t* __restrict__ row,
                                 const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
                                 uint32_t* __restrict__ order, uint32_t* __restrict__ bas,
-                                const uint32_t* __restrict__ lvl_off, uint32_t* tail) {
+                                const uint32_t* __restrict__ lvl_off, uint32_t* tail,
+                                int* __restrict__ flags) {
     uint32_t beg = lvl_off[L], end = lvl_off[L + 1];
     for (uint32_t idx = beg + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
          idx += gridDim.x * blockDim.x) {
@@ -276,8 +280,12 @@ __global__ void k_levels_expand(uint32_t L, const uint32_t* __restrict__ row,
             uint32_t d = col[s];
             if (next[d] == v && d != v) {
                 uint32_t pos = atomicAdd(tail, 1u);
-                order[pos] = d;
-                bas[d] = b;
+                if (pos < cap) {
+                    order[pos] = d;
+                    bas[d] = b;
+                } else {
+                    flags[kError] = 1;   // more visits than sites: receivers not a forest
+                }
             }
         }
     }
@@ -426,7 +434,9 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_outlet, n));
     FL_TRY(dalloc(&g->d_best, n));
     FL_TRY(dalloc(&g->d_flags, kNumFlags));
-    g->lvl_cap = n + 2;
+    // a forest on n sites has at most n levels; levels are launched in batches, so
+    // leave room for one batch past the deepest possible level
+    g->lvl_cap = n + kLevelBatch + 4;
     FL_TRY(dalloc(&g->d_lvl, g->lvl_cap));
     return FL_OK;
 }
@@ -540,10 +550,9 @@ int run_lakes(fl_graph* g) {
     return FL_OK;
 }
 
-constexpr uint32_t kLevelBatch = 64;
-
 // Basin levels from the outlets; returns the number of non-empty levels.
 int run_levels(fl_graph* g, uint32_t n_out, uint32_t* n_levels) {
+    FL_TRY(clear_flags(g));
     unsigned grid = 152 * 4;
     k_levels_init<<<blocks_for(n_out), kThreads, 0, g->stream>>>(n_out, g->d_outlets, g->d_order,
                                                                    g->d_bas, g->d_lvl, g->d_tail);
@@ -555,9 +564,9 @@ int run_levels(fl_graph* g, uint32_t n_out, uint32_t* n_levels) {
                 g_err = "basin depth exceeds the site count";
                 return FL_ERR_DEVICE_LIMIT;
             }
-            k_levels_expand<<<grid, kThreads, 0, g->stream>>>(L, g->d_row, g->d_col, g->d_next,
-                                                                g->d_order, g->d_bas, g->d_lvl,
-                                                                g->d_tail);
+            k_levels_expand<<<grid, kThreads, 0, g->stream>>>(L, g->n, g->d_row, g->d_col,
+                                                                g->d_next, g->d_order, g->d_bas,
+                                                                g->d_lvl, g->d_tail, g->d_flags);
             k_levels_close<<<1, 1, 0, g->stream>>>(L, g->d_lvl, g->d_tail);
         }
         FL_CU(cudaGetLastError());
@@ -574,6 +583,12 @@ int run_levels(fl_graph* g, uint32_t n_out, uint32_t* n_levels) {
     uint32_t nl = 0;
     while (nl < L + 1 && off[nl + 1] > off[nl]) ++nl;
     *n_levels = nl;
+    int h[kNumFlags];
+    FL_TRY(read_flags(g, h));
+    if (h[kError] || off[L] > g->n) {
+        g_err = "basin traversal visited more sites than exist";
+        return FL_ERR_DEVICE_LIMIT;
+    }
     return FL_OK;
 }
 
@@ -686,8 +701,16 @@ int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, co
         if (row_ptr[i + 1] < row_ptr[i]) { g_err = "row_ptr not monotone"; return FL_ERR_INVALID_ARGUMENT; }
     for (uint64_t s = 0; s < nnz; ++s)
         if (col[s] >= n || std::isnan(len[s])) { g_err = "column out of range or NaN length"; return FL_ERR_INVALID_ARGUMENT; }
-    for (uint32_t i = 0; i < n_default; ++i)
-        if (default_outlets[i] >= n) { g_err = "default outlet out of range"; return FL_ERR_INVALID_ARGUMENT; }
+    {
+        std::vector<uint8_t> seen(n, 0);
+        for (uint32_t i = 0; i < n_default; ++i) {
+            if (default_outlets[i] >= n || seen[default_outlets[i]]) {
+                g_err = "default outlet out of range or repeated";
+                return FL_ERR_INVALID_ARGUMENT;
+            }
+            seen[default_outlets[i]] = 1;
+        }
+    }
     fl_graph* g = new fl_graph();
     g->n = n;
     g->nnz = nnz;
