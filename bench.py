@@ -1,0 +1,296 @@
+"""Benchmark: fastlem generate() throughput (Msite-iters/s) on the 16M-site terrain.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one TerrainGenerator.generate() on the 16,000,000-site model with
+set_max_iteration(M) (M = --iters, default 8): the first iteration routes the
+initial-noise lakes, the rest are ordinary iterations.  Metric = sites x iterations
+executed / time.
+  value  device time of the iteration loop (CUDA events on the solver's stream), with
+         the graph and parameters resident in HBM; inputs (1.6 GB) are larger than L2.
+  e2e    the same work through the public API call with host arrays: parameter
+         upload, initial elevations, the loop and the elevation download, host-timed.
+Multi-GPU: a single terrain does not shard (replicas only); with N ranks each GPU
+solves its own copy, value = all ranks' site-iterations / max rank time.
+--impl reference times the CPU restatement of fastlem's own generate() (the oracle
+port; fastlem is Rust and no Rust toolchain exists here) on the same model, one
+bounded generate() per step, on rank 0 only.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Msite-iters/s at 16M sites"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="16m", choices=["small", "1m", "16m"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--iters", type=int, default=8, help="set_max_iteration per step")
+    ap.add_argument("--cpu-iters", type=int, default=1, help="iterations in the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while running."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpus):
+        self.gpus = gpus
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9 or not f[0].isdigit() or int(f[0]) >= self.gpus:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_workload(args):
+    from fastlem_gb300 import workloads
+    t = time.time()
+    w = workloads.CONFIGS[args.config](args.scale)
+    return w, time.time() - t
+
+
+def run_cpu_sample(w, iters):
+    """The oracle (CPU restatement of fastlem's generate) on this model, bounded to
+    `iters` iterations; returns (site-iterations per second, iterations, seconds)."""
+    from oracle import oracle as orc
+    from tests import graphs
+    p = w.params
+    r = orc.generate(graphs.from_model(w.model), p.base, p.erodibility, p.uplift, p.is_outlet,
+                     max_slope=p.max_slope, max_iter=iters)
+    return w.model.num() * r["iters"] / r["seconds"], r["iters"], r["seconds"]
+
+
+def workload_name(w):
+    c = w.config
+    return (f"{w.name}: {c['sites']:,} sites uniform in [0,{c['box']:g}]^2 seed {c['seed']}, "
+            f"relax {c['relax']}, outlets {c['outlets']}, erodibility {c['erodibility']}")
+
+
+def bench_reference(args, d):
+    if d.rank != 0:
+        return
+    from oracle import build as ob
+    ob.build()
+    w, build_s = make_workload(args)
+    n = w.model.num()
+    for _ in range(args.warmup):
+        run_cpu_sample(w, args.cpu_iters)
+    vals, secs, its = [], 0.0, 0
+    for _ in range(args.steps):
+        v, it, s = run_cpu_sample(w, args.cpu_iters)
+        vals.append(v)
+        secs += s
+        its += it
+    value = n * its / secs / 1e6
+    sample = (f"generate() with set_max_iteration({args.cpu_iters}) per step on the same "
+              f"{n:,}-site model, 1 thread")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Msite-iters/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(w), "iterations_per_step": args.cpu_iters},
+        "cpu_baseline": {"value": value, "unit": "Msite-iters/s", "cores": 1, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Msite-iters/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_gpu(args, d):
+    from fastlem_gb300 import TerrainGenerator, build as fb
+    from fastlem_gb300 import _lib
+    fb.build()
+    L = _lib.lib()
+    _lib.check(L.fl_select_device(d.local))
+    w, build_s = make_workload(args)
+    m, p = w.model, w.params
+    n = m.num()
+    h = m.handle()
+    gen = TerrainGenerator.default().set_model(m).set_parameters(p).set_max_iteration(args.iters)
+
+    for _ in range(args.warmup):
+        gen.generate()
+
+    # timed region: K steps, per-kernel CUDA-event timing on the solver stream
+    L.fl_graph_reset_stats(h)
+    _lib.check(L.fl_graph_set_timing(h, 1))
+    loop_ms, total_ms, iters = 0.0, 0.0, 0
+    d.barrier()
+    with ClockSampler(max(1, args.gpus)) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            gen.generate()
+            loop_ms += gen.last_loop_ms
+            total_ms += gen.last_total_ms
+            iters += gen.last_iterations
+        wall_ms = 1000 * (time.perf_counter() - t0)
+    d.barrier()
+    _lib.check(L.fl_graph_set_timing(h, 0))
+    stats = _lib.kernel_stats(h)
+
+    site_iters = d.sum(n * iters)
+    loop_max = d.max(loop_ms)
+    total_max = d.max(total_ms)
+    value = site_iters / (loop_max / 1000) / 1e6
+    e2e = site_iters / (total_max / 1000) / 1e6
+    launches = int(sum(v[0] for v in stats.values()))
+    if d.rank != 0:
+        return
+
+    # dominant kernel class by device time
+    dom = max(stats.items(), key=lambda kv: kv[1][1])
+    dname, (dl, dms, dbytes) = dom
+    peak, peak_kind = peak_hbm()
+    achieved = (dbytes / dl) / ((dms / dl) / 1000) / 1e9 if dl and dms else 0.0
+    roof = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "bytes_per_launch": dbytes / max(1, dl), "ms_per_launch": dms / max(1, dl),
+            "launches": dl}
+    share = {k: round(v[1] / max(1e-9, sum(x[1] for x in stats.values())), 4)
+             for k, v in stats.items() if v[0]}
+    cpu = None
+    if not args.no_cpu_baseline and args.gpus == 1:
+        from oracle import build as ob
+        ob.build()
+        v, it, s = run_cpu_sample(w, args.cpu_iters)
+        cpu = {"value": v / 1e6, "unit": "Msite-iters/s", "cores": 1, "kind": "port",
+               "sample": f"oracle generate() with set_max_iteration({it}) on the same {n:,}-site "
+                         f"model, {s:.1f} s, 1 thread", "host_cores": os.cpu_count()}
+    h2d = n * (8 + 8 + 8 + 1 + 8)   # base, erodibility, uplift, is_outlet, tan(max_slope)
+    d2h = n * 8
+    line = {
+        "metric": METRIC, "value": value, "unit": "Msite-iters/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": loop_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": workload_name(w), "iterations_per_step": args.iters,
+                   "site_iterations_per_step": n * iters // max(1, args.steps),
+                   "parallelism": f"replicas x{args.gpus}",
+                   "l2": "inputs larger than L2 (CSR and per-site arrays ~1.6 GB)",
+                   "graph_build_s": round(build_s, 1)},
+        "e2e": {"value": e2e, "unit": "Msite-iters/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+        "kernel_time_share": share,
+        "clocks": clocks.summary(),
+        "wall_ms_timed": wall_ms,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    d = Dist()
+    if args.impl == "reference":
+        bench_reference(args, d)
+    else:
+        bench_gpu(args, d)
+
+
+if __name__ == "__main__":
+    main()

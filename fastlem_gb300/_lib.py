@@ -27,7 +27,8 @@ FL_ERR_DEVICE_LIMIT = 23
 # Every symbol include/fastlem_gb300.h declares.
 EXPORTS = [
     "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
-    "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error",
+    "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
+    "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
     "fl_probe_rng_f64", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
 ]
@@ -62,6 +63,12 @@ def lib():
     L.fl_graph_num_slots.argtypes = [vp]
     L.fl_graph_num_slots.restype = c_u64
     L.fl_last_error.restype = ctypes.c_char_p
+    L.fl_select_device.argtypes = [c_int]
+    L.fl_graph_set_timing.argtypes = [vp, c_int]
+    L.fl_graph_reset_stats.argtypes = [vp]
+    L.fl_graph_reset_stats.restype = None
+    L.fl_num_kernel_classes.restype = c_u32
+    L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
     L.fl_probe_receivers.argtypes = [vp, vp, vp, vp, P(c_int)]
     L.fl_probe_lakes.argtypes = [vp, vp, c_u32, vp, vp, vp]
     L.fl_probe_tree_pass.argtypes = [vp, vp, c_u32, vp, vp, vp, vp, vp, vp, vp, P(c_int)]
@@ -105,3 +112,18 @@ def as_f64(a):
 
 def as_u8(a):
     return np.ascontiguousarray(a, dtype=np.uint8)
+
+
+def kernel_stats(handle):
+    """{class name: (launches, device_ms, algorithmic_bytes)} of a model handle."""
+    L = lib()
+    out = {}
+    for c in range(L.fl_num_kernel_classes()):
+        name = ctypes.c_char_p()
+        n = c_u64()
+        ms = c_dbl()
+        b = c_dbl()
+        check(L.fl_graph_kernel_stats(handle, c, ctypes.byref(name), ctypes.byref(n), ctypes.byref(ms),
+                                      ctypes.byref(b)))
+        out[name.value.decode()] = (n.value, ms.value, b.value)
+    return out

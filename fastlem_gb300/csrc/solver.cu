@@ -77,6 +77,13 @@ enum Flag { kHasLake = 0, kChanged = 1, kJumped = 2, kError = 3, kNumFlags = 8 }
 // Basin levels are expanded this many at a time between host checks.
 constexpr uint32_t kLevelBatch = 64;
 
+// Kernel classes for launch counting and per-class device timing.
+enum KClass { kcNoise = 0, kcReceivers, kcLabels, kcLakes, kcLevels, kcArea, kcTimeElev, kcMisc,
+              kcCount };
+const char* const kKClassName[kcCount] = {"initial_elevation", "receivers", "basin_labels",
+                                          "lake_reroute", "basin_levels", "drainage_area",
+                                          "response_elevation", "misc"};
+
 inline unsigned blocks_for(uint64_t n, int t = kThreads) {
     uint64_t b = (n + t - 1) / t;
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(b, 1u << 30));
@@ -388,6 +395,15 @@ struct fl_graph {
     unsigned long long* d_best = nullptr;
     int* d_flags = nullptr;
     uint32_t lvl_cap = 0;
+    int device = 0;
+    // instrumentation: launches / algorithmic bytes always, device time when enabled
+    bool timing = false;
+    uint64_t k_launches[kcCount] = {};
+    double k_ms[kcCount] = {};
+    double k_bytes[kcCount] = {};
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    cudaEvent_t ev_open = nullptr;
 };
 
 namespace {
@@ -406,11 +422,64 @@ void free_graph(fl_graph* g) {
                     g->d_tail, g->d_outlet, g->d_best, g->d_flags};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
+    for (auto& p : g->ev_pending) {
+        cudaEventDestroy(p.second.first);
+        cudaEventDestroy(p.second.second);
+    }
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }
+
+cudaEvent_t pooled_event(fl_graph* g) {
+    if (!g->ev_pool.empty()) {
+        cudaEvent_t e = g->ev_pool.back();
+        g->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Bracket one kernel launch: counts it, adds its algorithmic bytes, and (timing on)
+// records CUDA events on the solver's stream around it.
+void kbegin(fl_graph* g) {
+    if (g->timing) {
+        g->ev_open = pooled_event(g);
+        cudaEventRecord(g->ev_open, g->stream);
+    }
+}
+void kend(fl_graph* g, int cls, double bytes) {
+    g->k_launches[cls] += 1;
+    g->k_bytes[cls] += bytes;
+    if (g->timing && g->ev_open) {
+        cudaEvent_t e = pooled_event(g);
+        cudaEventRecord(e, g->stream);
+        g->ev_pending.push_back({cls, {g->ev_open, e}});
+        g->ev_open = nullptr;
+    }
+}
+// Folds finished event pairs into the per-class times (after a stream sync).
+void kresolve(fl_graph* g) {
+    for (auto& p : g->ev_pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess)
+            g->k_ms[p.first] += ms;
+        g->ev_pool.push_back(p.second.first);
+        g->ev_pool.push_back(p.second.second);
+    }
+    g->ev_pending.clear();
+}
+
+#define FL_LAUNCH(g, cls, bytes, ...) \
+    do {                              \
+        kbegin(g);                    \
+        __VA_ARGS__;                  \
+        kend(g, cls, (double)(bytes)); \
+    } while (0)
 
 int alloc_workspace(fl_graph* g) {
     uint32_t n = g->n;
@@ -499,9 +568,10 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
 // Receivers for the current elevations.  Returns has_lake in *has_lake.
 int run_receivers(fl_graph* g, int* has_lake) {
     FL_TRY(clear_flags(g));
-    k_receivers<<<blocks_for(g->n), kThreads, 0, g->stream>>>(g->n, g->d_row, g->d_col, g->d_len,
-                                                                g->d_elev, g->d_outlet, g->d_next,
-                                                                g->d_rlen, g->d_flags);
+    FL_LAUNCH(g, kcReceivers, 25.0 * g->n + 20.0 * g->nnz,
+              k_receivers<<<blocks_for(g->n), kThreads, 0, g->stream>>>(
+                  g->n, g->d_row, g->d_col, g->d_len, g->d_elev, g->d_outlet, g->d_next,
+                  g->d_rlen, g->d_flags));
     FL_CU(cudaGetLastError());
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
@@ -512,7 +582,8 @@ int run_receivers(fl_graph* g, int* has_lake) {
 // Basin labels of d_next into d_lab.
 int run_labels(fl_graph* g) {
     uint32_t n = g->n;
-    k_copy_u32<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_next, g->d_lab);
+    FL_LAUNCH(g, kcLabels, 8.0 * n,
+              k_copy_u32<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_next, g->d_lab));
     FL_CU(cudaGetLastError());
     for (int round = 0;; ++round) {
         if (round > 64) {
@@ -520,7 +591,9 @@ int run_labels(fl_graph* g) {
             return FL_ERR_DEVICE_LIMIT;
         }
         FL_TRY(clear_flags(g));
-        k_jump<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_lab, g->d_lab2, g->d_flags);
+        FL_LAUNCH(g, kcLabels, 12.0 * n,
+                  k_jump<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_lab, g->d_lab2,
+                                                                   g->d_flags));
         FL_CU(cudaGetLastError());
         std::swap(g->d_lab, g->d_lab2);
         int h[kNumFlags];
@@ -534,12 +607,16 @@ int run_labels(fl_graph* g) {
 int run_lakes(fl_graph* g) {
     uint32_t n = g->n;
     FL_TRY(clear_flags(g));
-    k_fill_u64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, (uint64_t*)g->d_best, kNoKey);
-    k_lake_keys<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_row, g->d_col, g->d_rank,
-                                                             g->d_lab, g->d_outlet, g->d_best);
-    k_lake_flip<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_row, g->d_col, g->d_len,
-                                                             g->d_best, g->d_sor, g->d_next,
-                                                             g->d_rlen, g->d_flags);
+    FL_LAUNCH(g, kcLakes, 8.0 * n,
+              k_fill_u64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, (uint64_t*)g->d_best,
+                                                                      kNoKey));
+    FL_LAUNCH(g, kcLakes, 12.0 * n + 8.0 * g->nnz,
+              k_lake_keys<<<blocks_for(n), kThreads, 0, g->stream>>>(
+                  n, g->d_row, g->d_col, g->d_rank, g->d_lab, g->d_outlet, g->d_best));
+    FL_LAUNCH(g, kcLakes, 8.0 * n,
+              k_lake_flip<<<blocks_for(n), kThreads, 0, g->stream>>>(
+                  n, g->d_row, g->d_col, g->d_len, g->d_best, g->d_sor, g->d_next, g->d_rlen,
+                  g->d_flags));
     FL_CU(cudaGetLastError());
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
@@ -554,8 +631,9 @@ int run_lakes(fl_graph* g) {
 int run_levels(fl_graph* g, uint32_t n_out, uint32_t* n_levels) {
     FL_TRY(clear_flags(g));
     unsigned grid = 152 * 4;
-    k_levels_init<<<blocks_for(n_out), kThreads, 0, g->stream>>>(n_out, g->d_outlets, g->d_order,
-                                                                   g->d_bas, g->d_lvl, g->d_tail);
+    FL_LAUNCH(g, kcLevels, 12.0 * n_out,
+              k_levels_init<<<blocks_for(n_out), kThreads, 0, g->stream>>>(
+                  n_out, g->d_outlets, g->d_order, g->d_bas, g->d_lvl, g->d_tail));
     FL_CU(cudaGetLastError());
     uint32_t L = 0;
     while (true) {
@@ -564,10 +642,12 @@ int run_levels(fl_graph* g, uint32_t n_out, uint32_t* n_levels) {
                 g_err = "basin depth exceeds the site count";
                 return FL_ERR_DEVICE_LIMIT;
             }
-            k_levels_expand<<<grid, kThreads, 0, g->stream>>>(L, g->n, g->d_row, g->d_col,
-                                                                g->d_next, g->d_order, g->d_bas,
-                                                                g->d_lvl, g->d_tail, g->d_flags);
-            k_levels_close<<<1, 1, 0, g->stream>>>(L, g->d_lvl, g->d_tail);
+            FL_LAUNCH(g, kcLevels, 0.0,
+                      k_levels_expand<<<grid, kThreads, 0, g->stream>>>(
+                          L, g->n, g->d_row, g->d_col, g->d_next, g->d_order, g->d_bas,
+                          g->d_lvl, g->d_tail, g->d_flags));
+            FL_LAUNCH(g, kcLevels, 0.0,
+                      k_levels_close<<<1, 1, 0, g->stream>>>(L, g->d_lvl, g->d_tail));
         }
         FL_CU(cudaGetLastError());
         // offsets of the last two levels written: lvl[L] .. lvl[L+1]
@@ -583,6 +663,8 @@ int run_levels(fl_graph* g, uint32_t n_out, uint32_t* n_levels) {
     uint32_t nl = 0;
     while (nl < L + 1 && off[nl + 1] > off[nl]) ++nl;
     *n_levels = nl;
+    // order 4+4, bas 4+4, row_ptr 8 per site; col 4 + next 4 per slot
+    g->k_bytes[kcLevels] += 24.0 * g->n + 8.0 * g->nnz;
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
     if (h[kError] || off[L] > g->n) {
@@ -597,16 +679,21 @@ int run_tree_pass(fl_graph* g, uint32_t n_out, int* changed) {
     uint32_t nl = 0;
     FL_TRY(run_levels(g, n_out, &nl));
     unsigned grid = 152 * 4;
+    // per-level bytes are not known on the host; the pass total is added to the
+    // last launch: order 4 + row_ptr 8 + area 8 + A 8+8 per site, col 4 + next 4 per slot
     for (uint32_t L = nl; L-- > 0;)
-        k_area_level<<<grid, kThreads, 0, g->stream>>>(L, g->d_row, g->d_col, g->d_next, g->d_order,
-                                                        g->d_lvl, g->d_area, g->d_A);
+        FL_LAUNCH(g, kcArea, L == 0 ? 36.0 * g->n + 8.0 * g->nnz : 0.0,
+                  k_area_level<<<grid, kThreads, 0, g->stream>>>(L, g->d_row, g->d_col,
+                                                                  g->d_next, g->d_order,
+                                                                  g->d_lvl, g->d_area, g->d_A));
     FL_CU(cudaGetLastError());
     FL_TRY(clear_flags(g));
+    // order 4, next 4, rlen 8, bas 4, A 8, k 8, u 8, tan 8, t 8+8, t_o 8, e_o 8, e 8+8 per site
     for (uint32_t L = 0; L < nl; ++L)
-        k_time_elev_level<<<grid, kThreads, 0, g->stream>>>(L, g->d_next, g->d_order, g->d_lvl,
-                                                             g->d_bas, g->d_A, g->d_rlen, g->d_k,
-                                                             g->d_u, g->d_tan, g->d_t, g->d_elev,
-                                                             g->d_flags);
+        FL_LAUNCH(g, kcTimeElev, L + 1 == nl ? 112.0 * g->n : 0.0,
+                  k_time_elev_level<<<grid, kThreads, 0, g->stream>>>(
+                      L, g->d_next, g->d_order, g->d_lvl, g->d_bas, g->d_A, g->d_rlen, g->d_k,
+                      g->d_u, g->d_tan, g->d_t, g->d_elev, g->d_flags));
     FL_CU(cudaGetLastError());
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
@@ -637,12 +724,15 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     if (!base || !k || !u || !is_outlet) return FL_ERR_PARAMETERS_NOT_SET;
     if (n_params != g->n) return FL_ERR_INVALID_NUM_PARAMETERS;
     if (!out_elev) return FL_ERR_INVALID_ARGUMENT;
+    FL_CU(cudaSetDevice(g->device));
     auto t_start = std::chrono::steady_clock::now();
     uint32_t n = g->n;
     std::vector<uint32_t> outlets = resolve_outlets(g, is_outlet);
     FL_TRY(upload_params(g, base, k, u, max_slope));
     FL_TRY(set_outlets(g, outlets, false));
-    k_initial_elevation<<<blocks_for((n + 7) / 8), kThreads, 0, g->stream>>>(n, g->d_base, g->d_elev);
+    FL_LAUNCH(g, kcNoise, 16.0 * n,
+              k_initial_elevation<<<blocks_for((n + 7) / 8), kThreads, 0, g->stream>>>(
+                  n, g->d_base, g->d_elev));
     FL_CU(cudaGetLastError());
     FL_CU(cudaEventRecord(g->ev0, g->stream));
     if (max_iter > 0xffffffffll) max_iter = 0xffffffffll;
@@ -663,6 +753,7 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     FL_CU(cudaEventRecord(g->ev1, g->stream));
     FL_CU(cudaMemcpyAsync(out_elev, g->d_elev, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
     FL_CU(cudaStreamSynchronize(g->stream));
+    kresolve(g);
     if (out_iters) *out_iters = iters;
     if (loop_ms) {
         float ms = 0;
@@ -712,6 +803,7 @@ int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, co
         }
     }
     fl_graph* g = new fl_graph();
+    if (cudaGetDevice(&g->device) != cudaSuccess) g->device = 0;
     g->n = n;
     g->nnz = nnz;
     g->h_row.assign(row_ptr, row_ptr + n + 1);
@@ -763,6 +855,7 @@ int fl_generate_timed(fl_graph* g, uint32_t n_params, const double* base,
 int fl_probe_receivers(fl_graph* g, const double* elev, const uint8_t* outlet_table,
                        uint32_t* next_out, int* has_lake) {
     if (!g) return FL_ERR_MODEL_NOT_SET;
+    FL_CU(cudaSetDevice(g->device));
     uint32_t n = g->n;
     FL_CU(cudaMemcpyAsync(g->d_elev, elev, n * 8ull, cudaMemcpyHostToDevice, g->stream));
     FL_CU(cudaMemcpyAsync(g->d_outlet, outlet_table, n, cudaMemcpyHostToDevice, g->stream));
@@ -777,6 +870,7 @@ int fl_probe_receivers(fl_graph* g, const double* elev, const uint8_t* outlet_ta
 int fl_probe_lakes(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
                    const uint32_t* next_in, uint32_t* next_out, uint32_t* label_out) {
     if (!g) return FL_ERR_MODEL_NOT_SET;
+    FL_CU(cudaSetDevice(g->device));
     uint32_t n = g->n;
     std::vector<uint32_t> o(outlets, outlets + n_outlets);
     FL_TRY(set_outlets(g, o, true));
@@ -798,6 +892,7 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
                        const double* max_slope, double* elev, double* drainage_out,
                        double* response_out, int* changed) {
     if (!g) return FL_ERR_MODEL_NOT_SET;
+    FL_CU(cudaSetDevice(g->device));
     uint32_t n = g->n;
     std::vector<uint32_t> o(outlets, outlets + n_outlets);
     FL_TRY(upload_params(g, nullptr, erodibility, uplift, max_slope));
@@ -832,6 +927,39 @@ int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
         g_err = "NaN edge length in the lake traversal";
         return FL_ERR_INVALID_ARGUMENT;
     }
+    return FL_OK;
+}
+
+int fl_select_device(int device) {
+    FL_CU(cudaSetDevice(device));
+    return FL_OK;
+}
+
+int fl_graph_set_timing(fl_graph* g, int enable) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    g->timing = enable != 0;
+    return FL_OK;
+}
+
+void fl_graph_reset_stats(fl_graph* g) {
+    if (!g) return;
+    for (int c = 0; c < kcCount; ++c) {
+        g->k_launches[c] = 0;
+        g->k_ms[c] = 0;
+        g->k_bytes[c] = 0;
+    }
+}
+
+uint32_t fl_num_kernel_classes(void) { return kcCount; }
+
+int fl_graph_kernel_stats(const fl_graph* g, uint32_t cls, const char** name, uint64_t* launches,
+                          double* device_ms, double* bytes) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    if (cls >= (uint32_t)kcCount) return FL_ERR_INVALID_ARGUMENT;
+    if (name) *name = kKClassName[cls];
+    if (launches) *launches = g->k_launches[cls];
+    if (device_ms) *device_ms = g->k_ms[cls];
+    if (bytes) *bytes = g->k_bytes[cls];
     return FL_OK;
 }
 

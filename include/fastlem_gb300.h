@@ -97,6 +97,20 @@ uint64_t fl_graph_num_slots(const fl_graph* g);
 /* Message for the last error on this thread ("" when none). */
 const char* fl_last_error(void);
 
+/* Make `device` current for this thread; fl_graph_create places the model on the
+ * current device and every later call on that model runs there. */
+int fl_select_device(int device);
+
+/* ---- instrumentation -------------------------------------------------------------
+ * Per kernel class: launches and algorithmic bytes are always counted; with timing
+ * enabled each launch is also bracketed by CUDA events on the model's stream and its
+ * device time accumulated.  Classes are numbered 0 .. fl_num_kernel_classes()-1. */
+int fl_graph_set_timing(fl_graph* g, int enable);
+void fl_graph_reset_stats(fl_graph* g);
+uint32_t fl_num_kernel_classes(void);
+int fl_graph_kernel_stats(const fl_graph* g, uint32_t cls, const char** name, uint64_t* launches,
+                          double* device_ms, double* bytes);
+
 /* ---- parity probes: one solver stage on host arrays (tests only) ---------------- */
 
 /* Steepest-descent receivers (lem/stream_tree.rs:109-137); outlet_table[i] != 0 keeps
