@@ -21,9 +21,9 @@ OUT_DIR = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(OUT_DIR, "libfastlem_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CUDA_SOURCES = ["solver.cu"]
+CUDA_SOURCES = ["solver.cu", "receivers.cu", "basin.cu"]
 CXX_SOURCES = ["builder.cpp", "prim_rank.cpp"]
-HEADERS = ["rng.h"]
+HEADERS = ["rng.h", "common.cuh", "kernels.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xptxas", "-v",

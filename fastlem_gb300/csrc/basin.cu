@@ -1,0 +1,660 @@
+// basin.cu -- drainage area, response time and elevation over the receiver forest
+// (src/lem/generator.rs:144-203, src/lem/drainage_basin.rs:13-46), bit-exact.
+//
+// The reference walks each outlet's basin breadth-first: drainage areas in reversed
+// BFS order (a site's donors are added in reverse adjacency order), then response
+// times and elevations in BFS order (parent before child).  Both are exact f64
+// recurrences along the river paths, and river paths are long: on the 16M-site
+// terrain the forest is ~24,000 levels deep with a few hundred sites per level, so
+// level-by-level processing is launch- and latency-bound.  The passes here are:
+//
+//  1. Kahn rounds (bottom-up, one cooperative kernel, grid barrier per round).
+//     Round r processes the sites of height r (all donors done): each pulls its
+//     donors' areas walking its adjacency row backwards, which reproduces the
+//     reference's addition order exactly.  Rounds stop once the ready frontier is
+//     narrower than `kahn_min_width`; what is left -- the skeleton -- is the deep
+//     trunk part of the rivers, a small fraction of the sites.
+//  2. Skeleton chains.  Every skeleton site with skeleton donors designates one of
+//     them (largest previous drainage area, i.e. the likely main stem) to continue
+//     its chain, so the skeleton splits into chains, one per skeleton leaf.  The
+//     chains are ranked by pointer jumping over the skeleton only and laid out
+//     contiguously; per site, the part of the pull that does not involve the chain
+//     predecessor is precomputed in parallel.
+//  3. Skeleton bottom-up: one thread per chain walks it from its leaf to its bottom
+//     doing only the dependent additions; a chain that reaches a confluence waits
+//     (bounded acquire/release flags) for the other chain's bottom.  All chains are
+//     co-resident, so the waits always end.
+//  4. w_v = (1 / (k_v * sqrt(A_v))) * len_v for all sites, in parallel.
+//  5. Skeleton top-down: the same chains from bottom to leaf, t_v = t_parent + w_v,
+//     elevation and slope clamp; a chain starts once its parent site is published.
+//  6. Remaining sites top-down by Kahn round, highest first (a site's receiver is
+//     higher, so it is done earlier).
+// Sites in components without an outlet are computed but never receive an
+// elevation, as in the reference (they are in no basin).
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace fl {
+namespace {
+
+// per-slot flags of the skeleton layout
+constexpr uint8_t kLeafSlot = 1;   // chain leaf: pre holds the complete area
+constexpr uint8_t kHasPost = 2;    // one addition after the chain predecessor
+constexpr uint8_t kSlow = 4;       // confluence or several post additions: full pull at walk time
+
+__device__ __forceinline__ double pull_area(uint32_t v, const uint32_t* __restrict__ row,
+                                            const uint32_t* __restrict__ col,
+                                            const uint32_t* __restrict__ next,
+                                            const double* __restrict__ area, const double* A) {
+    double a = area[v];
+    for (uint32_t s = row[v + 1]; s-- > row[v];) {
+        uint32_t d = col[s];
+        if (d != v && next[d] == v) a = __dadd_rn(a, __ldcg(&A[d]));
+    }
+    return a;
+}
+
+__global__ void k_count_donors(uint32_t n, const uint32_t* __restrict__ next,
+                               uint32_t* __restrict__ pending) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    uint32_t p = next[v];
+    if (p != v) atomicAdd(&pending[p], 1u);
+}
+
+__global__ void k_collect_leaves(uint32_t n, const uint32_t* __restrict__ pending,
+                                 uint32_t* __restrict__ order, uint32_t* __restrict__ counter) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    if (pending[v] == 0) order[atomicAdd(counter, 1u)] = v;
+}
+
+// Kahn rounds.  order[0, nleaves) holds the leaves; rounds append the next frontier
+// after the current one.  Writes hgt (round) and A of processed sites, the round
+// offsets roff[0..r_stop+1] and meta[kMetaRStop] = r_stop.
+__global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
+                       const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
+                       const double* __restrict__ area, double* A, uint32_t* pending,
+                       uint32_t* __restrict__ hgt, uint32_t* order, uint32_t* roff,
+                       uint32_t max_rounds, uint32_t min_width, uint32_t* meta, int* flags) {
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t beg = 0, end = ld_acquire_u(&meta[kMetaLeaves]);
+    uint32_t r = 0;
+    if (gtid == 0) {
+        roff[0] = 0;
+        roff[1] = end;
+    }
+    while (true) {
+        uint32_t width = end - beg;
+        if (width == 0 || width < min_width || r + 2 >= max_rounds) break;
+        uint32_t* cnt = &meta[kMetaCnt0 + (r % 3)];
+        if (gtid == 0) meta[kMetaCnt0 + ((r + 1) % 3)] = 0;
+        for (uint32_t idx = beg + gtid; idx < end; idx += stride) {
+            uint32_t v = __ldcg(&order[idx]);
+            A[v] = pull_area(v, row, col, next, area, A);
+            hgt[v] = r;
+            uint32_t p = next[v];
+            if (p != v && atomicSub(&pending[p], 1u) == 1u) {
+                uint32_t pos = end + atomicAdd(cnt, 1u);
+                if (pos < n) order[pos] = p;
+                else set_error(flags, kErrForest);
+            }
+        }
+        if (!grid_barrier(flags)) return;
+        beg = end;
+        end = end + ld_acquire_u(cnt);
+        ++r;
+        if (gtid == 0) roff[r + 1] = end;
+    }
+    if (gtid == 0) {
+        meta[kMetaRStop] = r;
+        meta[kMetaFrontBeg] = beg;
+        meta[kMetaFrontEnd] = end;
+    }
+}
+
+// ---- skeleton --------------------------------------------------------------------
+
+// The pointer-jumping result sits in ping-pong buffer meta[kMetaRankBuf].
+struct Ranks {
+    const uint32_t* ptr[2];
+    const uint32_t* dist[2];
+    __device__ __forceinline__ const uint32_t* P(const uint32_t* meta) const { return ptr[meta[kMetaRankBuf]]; }
+    __device__ __forceinline__ const uint32_t* D(const uint32_t* meta) const { return dist[meta[kMetaRankBuf]]; }
+};
+
+__global__ void k_s_collect(uint32_t n, const uint32_t* __restrict__ hgt,
+                            uint32_t* __restrict__ sid, uint32_t* __restrict__ slist,
+                            uint32_t* meta) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    if (hgt[v] == kNone) {
+        uint32_t k = atomicAdd(&meta[kMetaNs], 1u);
+        sid[v] = k;
+        slist[k] = v;
+    }
+}
+
+// For skeleton site p: the skeleton donor that continues p's chain (largest
+// previous drainage area, first in row order on ties), or none.
+__global__ void k_s_designate(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
+                              const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
+                              const double* __restrict__ A, const uint32_t* __restrict__ slist,
+                              uint32_t* __restrict__ desig, const uint32_t* meta) {
+    uint32_t ns = meta[kMetaNs];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
+        uint32_t p = slist[k];
+        uint32_t best = kNone;
+        double ba = 0.0;
+        for (uint32_t s = row[p]; s < row[p + 1]; ++s) {
+            uint32_t d = col[s];
+            if (d == p || next[d] != p || hgt[d] != kNone) continue;
+            double a = A[d];
+            if (best == kNone || a > ba) {
+                best = d;
+                ba = a;
+            }
+        }
+        desig[p] = best;
+    }
+}
+
+// Chain successor (toward the root) in skeleton-index space, for pointer jumping.
+__global__ void k_s_link(const uint32_t* __restrict__ next, const uint32_t* __restrict__ desig,
+                         const uint32_t* __restrict__ hgt, const uint32_t* __restrict__ sid,
+                         const uint32_t* __restrict__ slist, uint32_t* __restrict__ ptr,
+                         uint32_t* __restrict__ dist, const uint32_t* meta) {
+    uint32_t ns = meta[kMetaNs];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
+        uint32_t v = slist[k];
+        uint32_t p = next[v];
+        // a skeleton site's receiver is a skeleton site; desig is only written there
+        bool cont = (p != v) && hgt[p] == kNone && desig[p] == v;
+        ptr[k] = cont ? sid[p] : k;
+        dist[k] = cont ? 1u : 0u;
+    }
+}
+
+// Pointer jumping to the chain bottom: dist = sites below on the chain.
+__global__ void k_s_rank(uint32_t* ptr0, uint32_t* dist0, uint32_t* ptr1, uint32_t* dist1,
+                         uint32_t* meta, int* flags) {
+    const uint32_t ns = meta[kMetaNs];
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t* P[2] = {ptr0, ptr1};
+    uint32_t* D[2] = {dist0, dist1};
+    int cur = 0;
+    for (uint32_t round = 0; round < 64; ++round) {
+        uint32_t* jf = &meta[kMetaJump0 + (round % 3)];
+        if (gtid == 0) meta[kMetaJump0 + ((round + 1) % 3)] = 0;
+        bool changed = false;
+        for (uint32_t k = gtid; k < ns; k += stride) {
+            uint32_t p = __ldcg(&P[cur][k]);
+            uint32_t pp = __ldcg(&P[cur][p]);
+            D[cur ^ 1][k] = __ldcg(&D[cur][k]) + (p != k ? __ldcg(&D[cur][p]) : 0u);
+            P[cur ^ 1][k] = pp;
+            changed |= (pp != p);
+        }
+        if (changed) atomicOr(jf, 1u);
+        if (!grid_barrier(flags)) return;
+        cur ^= 1;
+        if (ld_acquire_u(jf) == 0) {
+            if (gtid == 0) meta[kMetaRankBuf] = cur;
+            return;
+        }
+    }
+    set_error(flags, kErrForest);
+}
+
+// Chain ids for chain bottoms.
+__global__ void k_s_bottoms(const uint32_t* __restrict__ slist, Ranks rk,
+                            uint32_t* __restrict__ cid, uint32_t* __restrict__ cbot,
+                            uint32_t max_chains, uint32_t* meta, int* flags) {
+    uint32_t ns = meta[kMetaNs];
+    const uint32_t* ptr = rk.P(meta);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
+        if (ptr[k] == k) {
+            uint32_t c = atomicAdd(&meta[kMetaChains], 1u);
+            if (c < max_chains) {
+                cid[k] = c;
+                cbot[c] = slist[k];
+            } else {
+                set_error(flags, kErrCapacity);
+            }
+        }
+    }
+}
+
+// Chain lengths from the skeleton leaves (the final Kahn frontier).
+__global__ void k_s_lengths(const uint32_t* __restrict__ order, const uint32_t* __restrict__ sid,
+                            Ranks rk, const uint32_t* __restrict__ cid, uint32_t* __restrict__ clen,
+                            uint32_t max_chains, const uint32_t* meta, const int* flags) {
+    if (flags[kError]) return;
+    uint32_t b = meta[kMetaFrontBeg], e = meta[kMetaFrontEnd];
+    const uint32_t* ptr = rk.P(meta);
+    const uint32_t* dist = rk.D(meta);
+    for (uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
+        uint32_t k = sid[order[i]];
+        uint32_t c = cid[ptr[k]];
+        if (c < max_chains) clen[c] = dist[k] + 1;
+    }
+}
+
+// Exclusive scan of chain lengths (single block).
+__global__ void k_s_scan(const uint32_t* __restrict__ clen, uint32_t* __restrict__ coff,
+                         const uint32_t* meta, const int* flags) {
+    __shared__ uint32_t part[1024];
+    if (flags[kError]) return;
+    uint32_t nc = meta[kMetaChains];
+    uint32_t per = (nc + blockDim.x - 1) / blockDim.x;
+    uint32_t b = threadIdx.x * per, e = min(nc, b + per);
+    uint32_t s = 0;
+    for (uint32_t i = b; i < e; ++i) s += clen[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (uint32_t i = b; i < e; ++i) {
+        coff[i] = run;
+        run += clen[i];
+    }
+}
+
+__global__ void k_s_layout(const uint32_t* __restrict__ slist, Ranks rk,
+                           const uint32_t* __restrict__ cid, const uint32_t* __restrict__ coff,
+                           uint32_t* __restrict__ layout, const uint32_t* meta, int* flags) {
+    if (flags[kError]) return;
+    uint32_t ns = meta[kMetaNs];
+    const uint32_t* ptr = rk.P(meta);
+    const uint32_t* dist = rk.D(meta);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
+        uint32_t q = coff[cid[ptr[k]]] + dist[k];
+        if (q < ns) layout[q] = slist[k];
+        else set_error(flags, kErrForest);
+    }
+}
+
+// Per skeleton site (layout slot q): the part of its pull that precedes the chain
+// predecessor (pre) and the single addition after it (post), or kSlow.  Also marks
+// the sites whose response time another chain waits for.
+__global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
+                            const uint32_t* __restrict__ col,
+                            const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
+                            const double* __restrict__ area, const double* __restrict__ A,
+                            const uint32_t* __restrict__ layout, const uint32_t* __restrict__ sid,
+                            Ranks rk, const uint32_t* __restrict__ cid,
+                            const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
+                            const uint32_t* __restrict__ cbot, double* __restrict__ pre,
+                            double* __restrict__ post, uint8_t* __restrict__ sflag,
+                            int* __restrict__ td_need, int stamp, const uint32_t* meta,
+                            int* flags) {
+    if (flags[kError]) return;
+    uint32_t ns = meta[kMetaNs];
+    const uint32_t* ptr = rk.P(meta);
+    uint32_t nc = meta[kMetaChains];
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x) {
+        uint32_t v = layout[q];
+        if (v >= n_sites) {
+            set_error(flags, kErrForest);
+            return;
+        }
+        uint32_t c = cid[ptr[sid[v]]];
+        uint32_t last = coff[c] + clen[c] - 1;
+        uint32_t heavy = q < last ? layout[q + 1] : kNone;
+        double a = area[v];
+        double ps = 0.0;
+        uint8_t f = (q == last) ? kLeafSlot : 0;
+        bool seen_heavy = false;
+        for (uint32_t s = row[v + 1]; s-- > row[v];) {
+            uint32_t d = col[s];
+            if (d == v || next[d] != v) continue;
+            if (d == heavy) {
+                seen_heavy = true;
+                continue;
+            }
+            if (hgt[d] == kNone) {          // another chain's bottom: resolved at walk time
+                f |= kSlow;
+                break;
+            }
+            double val = A[d];
+            if (!seen_heavy) {
+                a = __dadd_rn(a, val);
+            } else if (!(f & kHasPost)) {
+                ps = val;
+                f |= kHasPost;
+            } else {
+                f |= kSlow;
+                break;
+            }
+        }
+        pre[q] = a;
+        post[q] = ps;
+        sflag[q] = f;
+    }
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        uint32_t b = cbot[c];
+        uint32_t p = next[b];
+        if (p != b) td_need[p] = stamp;
+    }
+}
+
+// Full pull of v at walk time: heavy donor's value is x, other skeleton donors are
+// chain bottoms published through bu_done.
+__device__ double slow_pull(uint32_t v, uint32_t heavy, double x, const uint32_t* __restrict__ row,
+                            const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
+                            const uint32_t* __restrict__ hgt, const double* __restrict__ area,
+                            const double* A, const int* bu_done, int stamp, int* flags, bool* ok) {
+    double a = area[v];
+    for (uint32_t s = row[v + 1]; s-- > row[v];) {
+        uint32_t d = col[s];
+        if (d == v || next[d] != v) continue;
+        double val;
+        if (d == heavy) {
+            val = x;
+        } else {
+            if (hgt[d] == kNone) {
+                uint32_t spins = 0;
+                while (ld_acquire(&bu_done[d]) != stamp) {
+                    if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&flags[kError]))) {
+                        set_error(flags, kErrWait);
+                        *ok = false;
+                        return 0.0;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            val = __ldcg(&A[d]);
+        }
+        a = __dadd_rn(a, val);
+    }
+    return a;
+}
+
+__global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
+                              const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
+                              const double* __restrict__ area, double* A,
+                              const uint32_t* __restrict__ layout,
+                              const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
+                              const double* __restrict__ pre, const double* __restrict__ post,
+                              const uint8_t* __restrict__ sflag, int* bu_done, int stamp,
+                              const uint32_t* meta, int* flags) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= meta[kMetaChains] || flags[kError]) return;
+    const uint32_t off = coff[c];
+    uint32_t q = off + clen[c];
+    if (q > meta[kMetaNs] || q == off) {
+        set_error(flags, kErrForest);
+        return;
+    }
+    double x = 0.0;
+    uint32_t prev = kNone;
+    bool ok = true;
+    while (q-- > off) {
+        const uint32_t v = layout[q];
+        const uint8_t f = sflag[q];
+        if (f & kLeafSlot) {
+            x = pre[q];
+        } else if (!(f & kSlow)) {
+            x = __dadd_rn(pre[q], x);
+            if (f & kHasPost) x = __dadd_rn(x, post[q]);
+        } else {
+            x = slow_pull(v, prev, x, row, col, next, hgt, area, A, bu_done, stamp, flags, &ok);
+            if (!ok) return;
+        }
+        A[v] = x;
+        prev = v;
+    }
+    __threadfence();
+    st_release(&bu_done[prev], stamp);
+}
+
+// w_v = (1 / (k_v * sqrt(A_v))) * len_v  (generator.rs:172-173)
+__global__ void k_w(uint32_t n, const double* __restrict__ A, const double* __restrict__ kk,
+                    const double* __restrict__ rlen, double* __restrict__ w) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    double cel = __dmul_rn(kk[v], __dsqrt_rn(A[v]));
+    w[v] = __dmul_rn(__ddiv_rn(1.0, cel), rlen[v]);
+}
+
+struct TopDown {
+    const uint32_t* next;
+    const double* w;
+    const double* uu;
+    const double* tanms;
+    const double* rlen;
+    const uint8_t* outlet;
+    double* t;
+    double* elev;
+    uint32_t* bas;
+    int* flags;
+};
+
+// Response time, basin outlet and elevation of v given its receiver's values.
+// For a root, (tp, ep, o) are ignored.  Returns t_v; writes t, bas, elev.
+__device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t p, double tp,
+                                         uint32_t o, double to, double eo, double ep,
+                                         double* e_out) {
+    double tv;
+    double old_e = __ldcg(&td.elev[v]);
+    if (p == v) {                         // root: t = 0 + (0 + w), o = v
+        tv = plus_zero(plus_zero(td.w[v]));
+        o = td.outlet[v] ? v : kNone;
+        to = tv;
+        eo = old_e;
+        ep = old_e;
+    } else {
+        tv = plus_zero(__dadd_rn(tp, td.w[v]));
+    }
+    td.t[v] = tv;
+    td.bas[v] = o;
+    double ne = old_e;
+    if (o != kNone) {
+        double dt = __dsub_rn(tv, to);
+        ne = __dadd_rn(eo, __dmul_rn(td.uu[v], dt > 0.0 ? dt : 0.0));
+        double tn = td.tanms[v];
+        if (!isnan(tn)) {
+            double dist = td.rlen[v];
+            double slope = __ddiv_rn(__dsub_rn(ne, ep), dist);
+            if (slope > tn) ne = __dadd_rn(ep, __dmul_rn(tn, dist));
+        }
+        if (ne != old_e) td.flags[kChanged] = 1;
+        td.elev[v] = ne;
+    }
+    *e_out = ne;
+    return tv;
+}
+
+__global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
+                             const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
+                             const int* __restrict__ td_need, int* td_done, int stamp,
+                             const uint32_t* meta) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= meta[kMetaChains] || td.flags[kError]) return;
+    const uint32_t off = coff[c], end = off + clen[c];
+    if (end > meta[kMetaNs] || end == off) {
+        set_error(td.flags, kErrForest);
+        return;
+    }
+    uint32_t v = layout[off];
+    uint32_t p = td.next[v];
+    double tp = 0.0, ep = 0.0, to = 0.0, eo = 0.0;
+    uint32_t o = kNone;
+    if (p != v) {
+        uint32_t spins = 0;
+        while (ld_acquire(&td_done[p]) != stamp) {
+            if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
+                set_error(td.flags, kErrWait);
+                return;
+            }
+            __nanosleep(32);
+        }
+        tp = __ldcg(&td.t[p]);
+        ep = __ldcg(&td.elev[p]);
+        o = __ldcg(&td.bas[p]);
+        if (o != kNone) {
+            to = __ldcg(&td.t[o]);
+            eo = __ldcg(&td.elev[o]);
+        }
+    }
+    for (uint32_t q = off; q < end; ++q) {
+        v = layout[q];
+        double e;
+        double tv = settle(td, v, p, tp, o, to, eo, ep, &e);
+        if (p == v) {                     // chain bottom is a root
+            o = td.outlet[v] ? v : kNone;
+            to = tv;
+            eo = e;
+        }
+        if (td_need[v] == stamp) {
+            __threadfence();
+            st_release(&td_done[v], stamp);
+        }
+        tp = tv;
+        ep = e;
+        p = v;
+    }
+}
+
+// Top-down over the Kahn rounds, highest round first.
+__global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
+                               const uint32_t* __restrict__ roff, const uint32_t* meta) {
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    if (ld_acquire(&td.flags[kError])) return;
+    uint32_t rs = meta[kMetaRStop];
+    for (uint32_t r = rs; r-- > 0;) {
+        uint32_t b = roff[r], e = roff[r + 1];
+        for (uint32_t i = b + gtid; i < e; i += stride) {
+            uint32_t v = order[i];
+            uint32_t p = td.next[v];
+            double tp = 0.0, ep = 0.0, to = 0.0, eo = 0.0;
+            uint32_t o = kNone;
+            if (p != v) {
+                tp = __ldcg(&td.t[p]);
+                ep = __ldcg(&td.elev[p]);
+                o = __ldcg(&td.bas[p]);
+                if (o != kNone) {
+                    to = __ldcg(&td.t[o]);
+                    eo = __ldcg(&td.elev[o]);
+                }
+            }
+            double en;
+            settle(td, v, p, tp, o, to, eo, ep, &en);
+        }
+        if (!grid_barrier(td.flags)) return;
+    }
+}
+
+template <class K, class... Args>
+cudaError_t coop_launch(K kernel, unsigned grid, unsigned block, cudaStream_t st, Args... args) {
+    void* argv[] = {(void*)&args...};
+    return cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(block), argv, 0, st);
+}
+
+// Blocks of kThreads at which `kernel` is co-resident on the current device.
+unsigned coop_grid(const void* kernel, unsigned cap_per_sm) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
+    if (per < 1) per = 1;
+    return (unsigned)(sms * std::min<unsigned>((unsigned)per, cap_per_sm));
+}
+
+}  // namespace
+
+cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz) {
+    const uint32_t n = a.n;
+    const unsigned nb = (n + kThreads - 1) / kThreads;
+    const unsigned g_kahn = coop_grid((const void*)k_kahn, 4);
+    const unsigned g_rank = coop_grid((const void*)k_s_rank, 4);
+    const unsigned g_low = coop_grid((const void*)k_low_top_down, 4);
+    const unsigned g_chain = (a.kahn_min_width + kThreads - 1) / kThreads;
+    const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
+    Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
+    TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.t, a.elev, a.bas, a.flags};
+    cudaError_t e;
+
+    hk.begin(hk.ctx);
+    cudaMemsetAsync(a.pending, 0, n * 4ull, st);
+    cudaMemsetAsync(a.hgt, 0xff, n * 4ull, st);
+    cudaMemsetAsync(a.meta, 0, kMetaCount * 4ull, st);
+    k_count_donors<<<nb, kThreads, 0, st>>>(n, a.next, a.pending);
+    k_collect_leaves<<<nb, kThreads, 0, st>>>(n, a.pending, a.order, a.meta + kMetaLeaves);
+    hk.end(hk.ctx, kcBasinBuild, 20.0 * n);
+
+    // Kahn rounds: order 4 + next 4 + row 8 + area 8 + A 8 + hgt 4 + pending 4 per site,
+    // col 4 + next 4 per slot, donor areas 8 per site
+    hk.begin(hk.ctx);
+    e = coop_launch(k_kahn, g_kahn, kThreads, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
+                    a.hgt, a.order, a.roff, a.max_rounds, a.kahn_min_width, a.meta, a.flags);
+    hk.end(hk.ctx, kcKahn, 48.0 * n + 8.0 * nnz);
+    if (e != cudaSuccess) return e;
+
+    hk.begin(hk.ctx);
+    k_s_collect<<<nb, kThreads, 0, st>>>(n, a.hgt, a.sid, a.slist, a.meta);
+    k_s_designate<<<gs, kThreads, 0, st>>>(a.row, a.col, a.next, a.hgt, a.A, a.slist, a.desig,
+                                           a.meta);
+    k_s_link<<<gs, kThreads, 0, st>>>(a.next, a.desig, a.hgt, a.sid, a.slist, a.sptr0, a.sdist0,
+                                      a.meta);
+    hk.end(hk.ctx, kcBasinBuild, 4.0 * n);
+
+    hk.begin(hk.ctx);
+    e = coop_launch(k_s_rank, g_rank, kThreads, st, a.sptr0, a.sdist0, a.sptr1, a.sdist1, a.meta,
+                    a.flags);
+    hk.end(hk.ctx, kcSkelRank, 0.0);
+    if (e != cudaSuccess) return e;
+
+    hk.begin(hk.ctx);
+    k_s_bottoms<<<gs, kThreads, 0, st>>>(a.slist, rk, a.cid, a.cbot, a.kahn_min_width, a.meta,
+                                         a.flags);
+    k_s_lengths<<<gs, kThreads, 0, st>>>(a.order, a.sid, rk, a.cid, a.clen, a.kahn_min_width, a.meta,
+                                         a.flags);
+    k_s_scan<<<1, 1024, 0, st>>>(a.clen, a.coff, a.meta, a.flags);
+    k_s_layout<<<gs, kThreads, 0, st>>>(a.slist, rk, a.cid, a.coff, a.layout, a.meta, a.flags);
+    k_s_prepare<<<gs, kThreads, 0, st>>>(n, a.row, a.col, a.next, a.hgt, a.area, a.A, a.layout,
+                                         a.sid, rk, a.cid, a.coff, a.clen, a.cbot, a.pre, a.post,
+                                         a.sflag, a.td_need, a.stamp, a.meta, a.flags);
+    hk.end(hk.ctx, kcBasinBuild, 0.0);
+
+    hk.begin(hk.ctx);
+    e = coop_launch(k_s_bottom_up, g_chain, kThreads, st, a.row, a.col, a.next,
+                    (const uint32_t*)a.hgt, a.area, a.A, (const uint32_t*)a.layout,
+                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const double*)a.pre,
+                    (const double*)a.post, (const uint8_t*)a.sflag, a.bu_done, a.stamp,
+                    (const uint32_t*)a.meta, a.flags);
+    hk.end(hk.ctx, kcSkelUp, 0.0);
+    if (e != cudaSuccess) return e;
+
+    // w: A 8 + k 8 + rlen 8 + w 8 per site
+    hk.begin(hk.ctx);
+    k_w<<<nb, kThreads, 0, st>>>(n, a.A, a.k, a.rlen, a.w);
+    hk.end(hk.ctx, kcW, 32.0 * n);
+
+    hk.begin(hk.ctx);
+    e = coop_launch(k_s_top_down, g_chain, kThreads, st, td, (const uint32_t*)a.layout,
+                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const int*)a.td_need,
+                    a.td_done, a.stamp, (const uint32_t*)a.meta);
+    hk.end(hk.ctx, kcSkelDown, 0.0);
+    if (e != cudaSuccess) return e;
+
+    // top-down rounds: order 4, next 4, w 8, u 8, tan 8, rlen 8, elev 8+8, t 8, bas 4,
+    // parent t/elev/bas 20, outlet t/elev 16 per site
+    hk.begin(hk.ctx);
+    e = coop_launch(k_low_top_down, g_low, kThreads, st, td, (const uint32_t*)a.order,
+                    (const uint32_t*)a.roff, (const uint32_t*)a.meta);
+    hk.end(hk.ctx, kcLowDown, 112.0 * n);
+    return e;
+}
+
+}  // namespace fl

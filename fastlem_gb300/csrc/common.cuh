@@ -1,0 +1,102 @@
+// common.cuh -- shared device helpers of the GB300 solve.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fl {
+
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr unsigned long long kNoKey = ~0ull;
+constexpr int kThreads = 256;
+
+// Device status words (int32 slots of the solver's flag array).
+enum Flag {
+    kHasLake = 0,   // some non-outlet site has no lower neighbour
+    kChanged = 1,   // some elevation changed this iteration
+    kJumped = 2,    // a pointer-jumping round changed something
+    kError = 3,     // device-side limit hit (see kErr* codes)
+    kBarrier = 4,   // grid barrier arrival counter
+    kBarrierGen = 5,// grid barrier generation
+    kExact = 6,     // receiver scans that needed the exact f64 fallback
+    kNumFlags = 8
+};
+
+// Values stored in flags[kError].
+enum DeviceError {
+    kErrNone = 0,
+    kErrForest = 1,       // receivers do not form a forest (cycle / over-visit)
+    kErrBarrier = 2,      // a grid barrier wait ran out
+    kErrWait = 3,         // a chain hand-off wait ran out
+    kErrCapacity = 4,     // a fixed-size table overflowed
+};
+
+// Spin limits: a wait that exceeds them reports an error instead of hanging.
+constexpr uint32_t kSpinLimit = 1u << 24;
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_u(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void set_error(int* flags, int code) { atomicCAS(&flags[kError], 0, code); }
+
+// Grid-wide barrier for cooperative (co-resident) launches.  Every block's thread
+// 0 arrives on a counter; the last arrival bumps the generation.  Waits are bounded:
+// on timeout the error word is set and false is returned, after which callers
+// leave the kernel.
+__device__ __forceinline__ bool grid_barrier(int* flags) {
+    __syncthreads();
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        ok = 1;
+        int gen = ld_acquire(&flags[kBarrierGen]);
+        __threadfence();
+        unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+        int arrived = atomicAdd(&flags[kBarrier], 1);
+        if ((unsigned)arrived == nb - 1) {
+            atomicExch(&flags[kBarrier], 0);
+            __threadfence();
+            st_release(&flags[kBarrierGen], gen + 1);
+        } else {
+            uint32_t spins = 0;
+            while (ld_acquire(&flags[kBarrierGen]) == gen) {
+                if (++spins > kSpinLimit || ld_acquire(&flags[kError]) != 0) {
+                    set_error(flags, kErrBarrier);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+    }
+    __syncthreads();
+    return ok && ld_acquire(&flags[kError]) == 0;
+}
+
+// Waits (bounded) until *flag becomes nonzero.  Returns false on timeout / error.
+__device__ __forceinline__ bool wait_flag(const int* flag, int* flags) {
+    uint32_t spins = 0;
+    while (ld_acquire(flag) == 0) {
+        if (++spins > kSpinLimit) {
+            set_error(flags, kErrWait);
+            return false;
+        }
+        if ((spins & 255) == 0 && ld_acquire(&flags[kError]) != 0) return false;
+        __nanosleep(32);
+    }
+    return true;
+}
+
+// `0.0 + x` exactly as IEEE evaluates it: x itself, except that -0.0 becomes +0.0.
+__device__ __forceinline__ double plus_zero(double x) { return x == 0.0 ? 0.0 : x; }
+
+}  // namespace fl

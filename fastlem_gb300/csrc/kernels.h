@@ -1,0 +1,102 @@
+// kernels.h -- host-side entry points of the solver's CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fl {
+
+// Kernel classes for launch counting and per-class device timing.
+enum KClass {
+    kcNoise = 0,      // initial elevations
+    kcReceivers,      // steepest-descent receivers
+    kcLakes,          // basin labels + lake re-routing
+    kcBasinBuild,     // donor counts, leaves, skeleton collection / layout / preparation
+    kcKahn,           // bottom-up Kahn rounds (drainage area)
+    kcSkelRank,       // pointer jumping over the skeleton
+    kcSkelUp,         // skeleton chains bottom-up (drainage area)
+    kcW,              // 1 / (k sqrt(A)) * len
+    kcSkelDown,       // skeleton chains top-down (response time, elevation)
+    kcLowDown,        // Kahn rounds top-down (response time, elevation)
+    kcMisc,
+    kcCount
+};
+
+// Device-side bookkeeping words of one basin pass (uint32 slots of BasinArgs::meta).
+enum Meta {
+    kMetaLeaves = 0,   // number of leaves (Kahn round 0)
+    kMetaCnt0,         // rotating append counters of the Kahn rounds
+    kMetaCnt1,
+    kMetaCnt2,
+    kMetaRStop,        // number of Kahn rounds run
+    kMetaFrontBeg,     // the unprocessed frontier = skeleton leaves
+    kMetaFrontEnd,
+    kMetaNs,           // skeleton size
+    kMetaJump0,        // rotating "changed" words of the pointer jumping
+    kMetaJump1,
+    kMetaJump2,
+    kMetaRankBuf,      // which ping-pong buffer holds the ranks
+    kMetaChains,       // number of skeleton chains
+    kMetaCount
+};
+
+struct BasinArgs {
+    uint32_t n;
+    const uint32_t* row;
+    const uint32_t* col;
+    const double* area;
+    const uint32_t* next;
+    const double* rlen;
+    const double* k;
+    const double* u;
+    const double* tanms;
+    const uint8_t* outlet;
+    double* A;
+    double* t;
+    double* w;
+    double* elev;
+    uint32_t* bas;
+    uint32_t* pending;
+    uint32_t* hgt;
+    uint32_t* order;
+    uint32_t* roff;
+    uint32_t max_rounds;
+    uint32_t kahn_min_width;   // also the chain capacity
+    uint32_t* meta;
+    int* flags;
+    // skeleton
+    uint32_t* sid;
+    uint32_t* slist;
+    uint32_t* desig;
+    uint32_t* sptr0;
+    uint32_t* sdist0;
+    uint32_t* sptr1;
+    uint32_t* sdist1;
+    uint32_t* cid;
+    uint32_t* cbot;
+    uint32_t* clen;
+    uint32_t* coff;
+    uint32_t* layout;
+    double* pre;
+    double* post;
+    uint8_t* sflag;
+    int* bu_done;
+    int* td_need;
+    int* td_done;
+    int stamp;       // distinct per pass: hand-off flags never need clearing
+};
+
+// Instrumentation callbacks around each launch group.
+struct Hooks {
+    void* ctx;
+    void (*begin)(void* ctx);
+    void (*end)(void* ctx, int cls, double bytes);
+};
+
+void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const uint32_t* col,
+                      const double* len, const double* elev, const uint8_t* outlet,
+                      uint32_t* next, double* rlen, int* flags);
+
+// One drainage-area / response-time / elevation pass on final receivers.
+cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz);
+
+}  // namespace fl

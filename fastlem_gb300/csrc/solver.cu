@@ -11,13 +11,8 @@
 //                     touches it -- a packed 64-bit atomicMin of (heap rank << 32 | slot)
 //                     -- and the reversal of the receiver path from there to the lake
 //                     bottom (stream_tree.rs:175-243)
-//   3. levels         breadth-first levels of every outlet's basin over donors
-//                     (drainage_basin.rs:13-36)
-//   4. drainage area  bottom-up by level; each site pulls its donors' areas walking
-//                     its adjacency row backwards, which is exactly the addition
-//                     order of the reference's reversed BFS (generator.rs:154-159)
-//   5. response time  top-down by level (generator.rs:162-174)
-//      + elevation    (generator.rs:177-203), `changed` flag
+//   3. basin pass     drainage area bottom-up, response time and elevation top-down,
+//                     `changed` flag (generator.rs:144-203; basin.cu)
 // All FP64 arithmetic is written with explicit round-to-nearest intrinsics, so no
 // multiply-add is ever contracted and every value is bit-identical to the
 // reference's evaluation order.
@@ -33,7 +28,9 @@
 #include <string>
 #include <vector>
 
+#include "common.cuh"
 #include "fastlem_gb300.h"
+#include "kernels.h"
 #include "rng.h"
 
 namespace fl {
@@ -43,10 +40,14 @@ bool lake_heap_rank(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, co
 
 namespace {
 
-constexpr uint32_t kNone = 0xffffffffu;
-constexpr uint64_t kNoKey = ~0ull;
+using fl::kNone;
+using fl::kNoKey;
+using fl::kThreads;
+using namespace fl;
 constexpr double kEpsilon = 2.220446049250313e-16;   // f64::EPSILON
-constexpr int kThreads = 256;
+// Kahn rounds stop when the ready frontier is narrower than this; it also bounds
+// the number of skeleton chains (one co-resident thread each).
+constexpr uint32_t kKahnMinWidth = 8192;
 
 thread_local std::string g_err;
 
@@ -70,19 +71,6 @@ void set_err(const char* what, cudaError_t e) {
         int rc_ = (expr);       \
         if (rc_ != FL_OK) return rc_; \
     } while (0)
-
-// Device flags (int32 slots of fl_graph::d_flags).
-enum Flag { kHasLake = 0, kChanged = 1, kJumped = 2, kError = 3, kNumFlags = 8 };
-
-// Basin levels are expanded this many at a time between host checks.
-constexpr uint32_t kLevelBatch = 64;
-
-// Kernel classes for launch counting and per-class device timing.
-enum KClass { kcNoise = 0, kcReceivers, kcLabels, kcLakes, kcLevels, kcArea, kcTimeElev, kcMisc,
-              kcCount };
-const char* const kKClassName[kcCount] = {"initial_elevation", "receivers", "basin_labels",
-                                          "lake_reroute", "basin_levels", "drainage_area",
-                                          "response_elevation", "misc"};
 
 inline unsigned blocks_for(uint64_t n, int t = kThreads) {
     uint64_t b = (n + t - 1) / t;
@@ -136,48 +124,6 @@ __device__ __forceinline__ double edge_len_or_one(const uint32_t* __restrict__ r
     return 1.0;
 }
 
-// Steepest-descent receivers (stream_tree.rs:109-137).  rlen[i] = length of the
-// edge to the receiver (1.0 when next[i] == i).  Flags kHasLake when a non-outlet
-// site keeps itself as receiver.
-__global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
-                            const uint32_t* __restrict__ col, const double* __restrict__ len,
-                            const double* __restrict__ elev, const uint8_t* __restrict__ outlet,
-                            uint32_t* __restrict__ next, double* __restrict__ rlen,
-                            int* __restrict__ flags) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (outlet[i]) {
-        next[i] = i;
-        rlen[i] = 1.0;
-        return;
-    }
-    const double ei = elev[i];
-    double steepest = 0.0;
-    uint32_t best = i, best_slot = kNone;
-    const uint32_t s0 = row[i], s1 = row[i + 1];
-    for (uint32_t s = s0; s < s1; ++s) {
-        uint32_t j = col[s];
-        double ej = elev[j];
-        if (ei > ej) {
-            double slope = __ddiv_rn(__dsub_rn(ei, ej), len[s]);
-            if (slope > steepest) {
-                steepest = slope;
-                best = j;
-                best_slot = s;
-            }
-        }
-    }
-    next[i] = best;
-    if (best_slot == kNone) {
-        rlen[i] = 1.0;
-        flags[kHasLake] = 1;
-    } else {
-        uint32_t s = s0;
-        while (col[s] != best) ++s;   // first occurrence, as has_edge reports it
-        rlen[i] = len[s];
-    }
-}
-
 __global__ void k_copy_u32(uint32_t n, const uint32_t* __restrict__ a, uint32_t* __restrict__ b) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = a[i];
@@ -193,7 +139,7 @@ __global__ void k_jump(uint32_t n, const uint32_t* __restrict__ lab_in,
     uint32_t l = lab_in[i];
     uint32_t ll = lab_in[l];
     lab_out[i] = ll;
-    if (ll != l) flags[kJumped] = 1;
+    if (ll != l) flags[fl::kJumped] = 1;
 }
 
 __global__ void k_fill_u64(uint32_t n, uint64_t* __restrict__ a, uint64_t v) {
@@ -240,7 +186,7 @@ __global__ void k_lake_flip(uint32_t n, const uint32_t* __restrict__ row,
     uint32_t k = j, nk = v;
     for (uint32_t steps = 0;; ++steps) {
         if (steps > n) {             // a cycle: cannot happen on a descent forest
-            flags[kError] = 1;
+            set_error(flags, kErrForest);
             return;
         }
         uint32_t nx = next[k];
@@ -254,111 +200,6 @@ __global__ void k_lake_flip(uint32_t n, const uint32_t* __restrict__ row,
     rlen[k] = edge_len_or_one(row, col, len, k, nk);
 }
 
-// Level 0 of the basin traversal: the outlets, each its own basin.
-__global__ void k_levels_init(uint32_t n_out, const uint32_t* __restrict__ outlets,
-                              uint32_t* __restrict__ order, uint32_t* __restrict__ bas,
-                              uint32_t* __restrict__ lvl_off, uint32_t* __restrict__ tail) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n_out) {
-        uint32_t o = outlets[i];
-        order[i] = o;
-        bas[o] = o;
-    }
-    if (i == 0) {
-        lvl_off[0] = 0;
-        lvl_off[1] = n_out;
-        *tail = n_out;
-    }
-}
-
-// Expand level L into level L+1: every donor d of a level-L site v (next[d] == v,
-// drainage_basin.rs:267-271) is appended.  Grid-stride over the level.
-__global__ void k_levels_expand(uint32_t L, uint32_t cap, const uint32_t* __restrict__ row,
-                                const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
-                                uint32_t* __restrict__ order, uint32_t* __restrict__ bas,
-                                const uint32_t* __restrict__ lvl_off, uint32_t* tail,
-                                int* __restrict__ flags) {
-    uint32_t beg = lvl_off[L], end = lvl_off[L + 1];
-    for (uint32_t idx = beg + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
-         idx += gridDim.x * blockDim.x) {
-        uint32_t v = order[idx];
-        uint32_t b = bas[v];
-        for (uint32_t s = row[v], e = row[v + 1]; s < e; ++s) {
-            uint32_t d = col[s];
-            if (next[d] == v && d != v) {
-                uint32_t pos = atomicAdd(tail, 1u);
-                if (pos < cap) {
-                    order[pos] = d;
-                    bas[d] = b;
-                } else {
-                    flags[kError] = 1;   // more visits than sites: receivers not a forest
-                }
-            }
-        }
-    }
-}
-
-__global__ void k_levels_close(uint32_t L, uint32_t* __restrict__ lvl_off,
-                               const uint32_t* __restrict__ tail) {
-    lvl_off[L + 2] = *tail;
-}
-
-// Drainage area of level-L sites: A_v = a_v + A_{d_m} + ... + A_{d_1}, donors taken
-// in reverse adjacency order (the reference's reversed BFS, generator.rs:154-159).
-__global__ void k_area_level(uint32_t L, const uint32_t* __restrict__ row,
-                             const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
-                             const uint32_t* __restrict__ order, const uint32_t* __restrict__ lvl_off,
-                             const double* __restrict__ area, double* A) {
-    uint32_t beg = lvl_off[L], end = lvl_off[L + 1];
-    for (uint32_t idx = beg + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
-         idx += gridDim.x * blockDim.x) {
-        uint32_t v = order[idx];
-        double a = area[v];
-        for (uint32_t s = row[v + 1]; s-- > row[v];) {
-            uint32_t d = col[s];
-            if (next[d] == v && d != v) a = __dadd_rn(a, A[d]);
-        }
-        A[v] = a;
-    }
-}
-
-// Response time and elevation of level-L sites (generator.rs:162-203):
-//   t_v = 0 + (t_next + (1 / (k_v * sqrt(A_v))) * len)      (outlet: t_next = 0, len = 1)
-//   e_v = e_o + u_v * max(t_v - t_o, 0), then the optional slope clamp against the
-//   receiver's already-updated elevation.
-__global__ void k_time_elev_level(uint32_t L, const uint32_t* __restrict__ next,
-                                  const uint32_t* __restrict__ order,
-                                  const uint32_t* __restrict__ lvl_off,
-                                  const uint32_t* __restrict__ bas, const double* __restrict__ A,
-                                  const double* __restrict__ rlen, const double* __restrict__ kk,
-                                  const double* __restrict__ uu, const double* __restrict__ tanms,
-                                  double* t, double* elev, int* flags) {
-    uint32_t beg = lvl_off[L], end = lvl_off[L + 1];
-    for (uint32_t idx = beg + blockIdx.x * blockDim.x + threadIdx.x; idx < end;
-         idx += gridDim.x * blockDim.x) {
-        uint32_t v = order[idx];
-        uint32_t j = next[v];
-        double dist = rlen[v];
-        double tj = (j == v) ? 0.0 : t[j];
-        double cel = __dmul_rn(kk[v], __dsqrt_rn(A[v]));
-        double tv = __dadd_rn(0.0, __dadd_rn(tj, __dmul_rn(__ddiv_rn(1.0, cel), dist)));
-        t[v] = tv;
-        uint32_t o = bas[v];
-        double to = (o == v) ? tv : t[o];
-        double dt = __dsub_rn(tv, to);
-        double old_e = elev[v];
-        double ne = __dadd_rn(elev[o], __dmul_rn(uu[v], dt > 0.0 ? dt : 0.0));
-        double tn = tanms[v];
-        if (!isnan(tn)) {
-            double ej = (j == v) ? old_e : elev[j];
-            double slope = __ddiv_rn(__dsub_rn(ne, ej), dist);
-            if (slope > tn) ne = __dadd_rn(ej, __dmul_rn(tn, dist));
-        }
-        if (ne != old_e) flags[kChanged] = 1;
-        elev[v] = ne;
-    }
-}
-
 __global__ void k_fill_f64(uint32_t n, double* __restrict__ a, const double* __restrict__ src) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = src ? src[i] : 0.0;
@@ -369,9 +210,14 @@ __global__ void k_fill_f64(uint32_t n, double* __restrict__ a, const double* __r
 // ---------------------------------------------------------------------------
 // Model handle
 // ---------------------------------------------------------------------------
+const char* const kKClassName[kcCount] = {
+    "initial_elevation", "receivers", "lake_reroute", "basin_build", "kahn_rounds",
+    "skeleton_rank", "skeleton_up", "response_w", "skeleton_down", "rounds_down", "misc"};
+
 struct fl_graph {
     uint32_t n = 0;
     uint64_t nnz = 0;
+    int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // host copies used by the host-side lake-heap rank
@@ -383,19 +229,28 @@ struct fl_graph {
     bool rank_valid = false;
     bool rank_uploaded = false;
     std::vector<uint32_t> h_rank;
-    // device arrays
+    // model (device)
     uint32_t *d_row = nullptr, *d_col = nullptr;
     double *d_len = nullptr, *d_area = nullptr;
-    double *d_k = nullptr, *d_u = nullptr, *d_tan = nullptr, *d_elev = nullptr, *d_A = nullptr,
-           *d_t = nullptr, *d_rlen = nullptr, *d_base = nullptr;
+    // parameters and iteration state (device)
+    double *d_k = nullptr, *d_u = nullptr, *d_tan = nullptr, *d_base = nullptr, *d_elev = nullptr,
+           *d_A = nullptr, *d_t = nullptr, *d_w = nullptr, *d_rlen = nullptr;
     uint32_t *d_next = nullptr, *d_lab = nullptr, *d_lab2 = nullptr, *d_rank = nullptr,
-             *d_sor = nullptr, *d_bas = nullptr, *d_order = nullptr, *d_lvl = nullptr,
-             *d_outlets = nullptr, *d_tail = nullptr;
+             *d_sor = nullptr, *d_outlets = nullptr, *d_bas = nullptr;
     uint8_t* d_outlet = nullptr;
     unsigned long long* d_best = nullptr;
     int* d_flags = nullptr;
-    uint32_t lvl_cap = 0;
-    int device = 0;
+    // basin pass workspace (device)
+    uint32_t *d_pending = nullptr, *d_hgt = nullptr, *d_order = nullptr, *d_roff = nullptr,
+             *d_meta = nullptr, *d_sid = nullptr, *d_slist = nullptr, *d_desig = nullptr,
+             *d_sptr0 = nullptr, *d_sdist0 = nullptr, *d_sptr1 = nullptr, *d_sdist1 = nullptr,
+             *d_cid = nullptr, *d_cbot = nullptr, *d_clen = nullptr, *d_coff = nullptr,
+             *d_layout = nullptr;
+    double *d_pre = nullptr, *d_post = nullptr;
+    uint8_t* d_sflag = nullptr;
+    int *d_bu_done = nullptr, *d_td_need = nullptr, *d_td_done = nullptr;
+    uint32_t max_rounds = 0, kahn_min_width = kKahnMinWidth;
+    int stamp = 0;
     // instrumentation: launches / algorithmic bytes always, device time when enabled
     bool timing = false;
     uint64_t k_launches[kcCount] = {};
@@ -416,10 +271,13 @@ int dalloc(T** p, uint64_t count) {
 
 void free_graph(fl_graph* g) {
     if (!g) return;
-    void* ptrs[] = {g->d_row, g->d_col, g->d_len, g->d_area, g->d_k, g->d_u, g->d_tan, g->d_elev,
-                    g->d_A, g->d_t, g->d_rlen, g->d_base, g->d_next, g->d_lab, g->d_lab2,
-                    g->d_rank, g->d_sor, g->d_bas, g->d_order, g->d_lvl, g->d_outlets,
-                    g->d_tail, g->d_outlet, g->d_best, g->d_flags};
+    void* ptrs[] = {g->d_row, g->d_col, g->d_len, g->d_area, g->d_k, g->d_u, g->d_tan, g->d_base,
+                    g->d_elev, g->d_A, g->d_t, g->d_w, g->d_rlen, g->d_next, g->d_lab, g->d_lab2,
+                    g->d_rank, g->d_sor, g->d_outlets, g->d_bas, g->d_outlet, g->d_best,
+                    g->d_flags, g->d_pending, g->d_hgt, g->d_order, g->d_roff, g->d_meta,
+                    g->d_sid, g->d_slist, g->d_desig, g->d_sptr0, g->d_sdist0, g->d_sptr1,
+                    g->d_sdist1, g->d_cid, g->d_cbot, g->d_clen, g->d_coff, g->d_layout,
+                    g->d_pre, g->d_post, g->d_sflag, g->d_bu_done, g->d_td_need, g->d_td_done};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -444,15 +302,17 @@ cudaEvent_t pooled_event(fl_graph* g) {
     return e;
 }
 
-// Bracket one kernel launch: counts it, adds its algorithmic bytes, and (timing on)
-// records CUDA events on the solver's stream around it.
-void kbegin(fl_graph* g) {
+// Bracket a launch group: counts it, adds its algorithmic bytes and, with timing
+// on, records CUDA events on the model's stream around it.
+void kbegin(void* ctx) {
+    fl_graph* g = (fl_graph*)ctx;
     if (g->timing) {
         g->ev_open = pooled_event(g);
         cudaEventRecord(g->ev_open, g->stream);
     }
 }
-void kend(fl_graph* g, int cls, double bytes) {
+void kend(void* ctx, int cls, double bytes) {
+    fl_graph* g = (fl_graph*)ctx;
     g->k_launches[cls] += 1;
     g->k_bytes[cls] += bytes;
     if (g->timing && g->ev_open) {
@@ -482,31 +342,55 @@ void kresolve(fl_graph* g) {
     } while (0)
 
 int alloc_workspace(fl_graph* g) {
-    uint32_t n = g->n;
+    const uint32_t n = g->n;
     FL_TRY(dalloc(&g->d_k, n));
     FL_TRY(dalloc(&g->d_u, n));
     FL_TRY(dalloc(&g->d_tan, n));
+    FL_TRY(dalloc(&g->d_base, n));
     FL_TRY(dalloc(&g->d_elev, n));
     FL_TRY(dalloc(&g->d_A, n));
     FL_TRY(dalloc(&g->d_t, n));
+    FL_TRY(dalloc(&g->d_w, n));
     FL_TRY(dalloc(&g->d_rlen, n));
-    FL_TRY(dalloc(&g->d_base, n));
     FL_TRY(dalloc(&g->d_next, n));
     FL_TRY(dalloc(&g->d_lab, n));
     FL_TRY(dalloc(&g->d_lab2, n));
     FL_TRY(dalloc(&g->d_rank, n));
     FL_TRY(dalloc(&g->d_sor, n));
-    FL_TRY(dalloc(&g->d_bas, n));
-    FL_TRY(dalloc(&g->d_order, n));
     FL_TRY(dalloc(&g->d_outlets, n));
-    FL_TRY(dalloc(&g->d_tail, 1));
+    FL_TRY(dalloc(&g->d_bas, n));
     FL_TRY(dalloc(&g->d_outlet, n));
     FL_TRY(dalloc(&g->d_best, n));
     FL_TRY(dalloc(&g->d_flags, kNumFlags));
-    // a forest on n sites has at most n levels; levels are launched in batches, so
-    // leave room for one batch past the deepest possible level
-    g->lvl_cap = n + kLevelBatch + 4;
-    FL_TRY(dalloc(&g->d_lvl, g->lvl_cap));
+    FL_TRY(dalloc(&g->d_pending, n));
+    FL_TRY(dalloc(&g->d_hgt, n));
+    FL_TRY(dalloc(&g->d_order, n));
+    // each Kahn round retires at least kahn_min_width sites
+    g->max_rounds = n / g->kahn_min_width + 64;
+    FL_TRY(dalloc(&g->d_roff, g->max_rounds + 2));
+    FL_TRY(dalloc(&g->d_meta, kMetaCount));
+    FL_TRY(dalloc(&g->d_sid, n));
+    FL_TRY(dalloc(&g->d_slist, n));
+    FL_TRY(dalloc(&g->d_desig, n));
+    FL_TRY(dalloc(&g->d_sptr0, n));
+    FL_TRY(dalloc(&g->d_sdist0, n));
+    FL_TRY(dalloc(&g->d_sptr1, n));
+    FL_TRY(dalloc(&g->d_sdist1, n));
+    FL_TRY(dalloc(&g->d_cid, n));
+    FL_TRY(dalloc(&g->d_cbot, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_clen, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_coff, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_layout, n));
+    FL_TRY(dalloc(&g->d_pre, n));
+    FL_TRY(dalloc(&g->d_post, n));
+    FL_TRY(dalloc(&g->d_sflag, n));
+    FL_TRY(dalloc(&g->d_bu_done, n));
+    FL_TRY(dalloc(&g->d_td_need, n));
+    FL_TRY(dalloc(&g->d_td_done, n));
+    FL_CU(cudaMemset(g->d_bu_done, 0, n * 4ull));
+    FL_CU(cudaMemset(g->d_td_need, 0, n * 4ull));
+    FL_CU(cudaMemset(g->d_td_done, 0, n * 4ull));
+    FL_CU(cudaMemset(g->d_flags, 0, kNumFlags * 4ull));
     return FL_OK;
 }
 
@@ -516,9 +400,21 @@ int read_flags(fl_graph* g, int* h) {
     return FL_OK;
 }
 
+// Clears the per-iteration status words (not the barrier words, which the grid
+// barrier leaves consistent).
 int clear_flags(fl_graph* g) {
-    FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
+    FL_CU(cudaMemsetAsync(g->d_flags, 0, 4 * sizeof(int), g->stream));
+    FL_CU(cudaMemsetAsync(g->d_flags + kExact, 0, sizeof(int), g->stream));
     return FL_OK;
+}
+
+int device_error(const int* h) {
+    static const char* what[] = {"", "receivers do not form a forest", "grid barrier timed out",
+                                 "chain hand-off timed out", "skeleton chain table overflow"};
+    int c = h[kError];
+    if (c <= 0 || c > 4) return FL_OK;
+    g_err = what[c];
+    return FL_ERR_DEVICE_LIMIT;
 }
 
 // Outlet list as generate() resolves it (generator.rs:120-132).
@@ -565,13 +461,12 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
     return FL_OK;
 }
 
-// Receivers for the current elevations.  Returns has_lake in *has_lake.
+// Receivers for the current elevations; *has_lake from the device flag.
 int run_receivers(fl_graph* g, int* has_lake) {
     FL_TRY(clear_flags(g));
     FL_LAUNCH(g, kcReceivers, 25.0 * g->n + 20.0 * g->nnz,
-              k_receivers<<<blocks_for(g->n), kThreads, 0, g->stream>>>(
-                  g->n, g->d_row, g->d_col, g->d_len, g->d_elev, g->d_outlet, g->d_next,
-                  g->d_rlen, g->d_flags));
+              fl::launch_receivers(g->stream, g->n, g->d_row, g->d_col, g->d_len, g->d_elev,
+                                   g->d_outlet, g->d_next, g->d_rlen, g->d_flags));
     FL_CU(cudaGetLastError());
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
@@ -579,10 +474,10 @@ int run_receivers(fl_graph* g, int* has_lake) {
     return FL_OK;
 }
 
-// Basin labels of d_next into d_lab.
+// Basin labels of d_next into d_lab (pointer jumping).
 int run_labels(fl_graph* g) {
     uint32_t n = g->n;
-    FL_LAUNCH(g, kcLabels, 8.0 * n,
+    FL_LAUNCH(g, kcLakes, 8.0 * n,
               k_copy_u32<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_next, g->d_lab));
     FL_CU(cudaGetLastError());
     for (int round = 0;; ++round) {
@@ -591,7 +486,7 @@ int run_labels(fl_graph* g) {
             return FL_ERR_DEVICE_LIMIT;
         }
         FL_TRY(clear_flags(g));
-        FL_LAUNCH(g, kcLabels, 12.0 * n,
+        FL_LAUNCH(g, kcLakes, 12.0 * n,
                   k_jump<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_lab, g->d_lab2,
                                                                    g->d_flags));
         FL_CU(cudaGetLastError());
@@ -620,83 +515,71 @@ int run_lakes(fl_graph* g) {
     FL_CU(cudaGetLastError());
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
-    if (h[kError]) {
-        g_err = "lake re-routing walked a cycle";
-        return FL_ERR_DEVICE_LIMIT;
-    }
-    return FL_OK;
+    return device_error(h);
 }
 
-// Basin levels from the outlets; returns the number of non-empty levels.
-int run_levels(fl_graph* g, uint32_t n_out, uint32_t* n_levels) {
+// Drainage areas, response times, elevations on final receivers; *changed.
+int run_basin_pass(fl_graph* g, int* changed) {
     FL_TRY(clear_flags(g));
-    unsigned grid = 152 * 4;
-    FL_LAUNCH(g, kcLevels, 12.0 * n_out,
-              k_levels_init<<<blocks_for(n_out), kThreads, 0, g->stream>>>(
-                  n_out, g->d_outlets, g->d_order, g->d_bas, g->d_lvl, g->d_tail));
-    FL_CU(cudaGetLastError());
-    uint32_t L = 0;
-    while (true) {
-        for (uint32_t b = 0; b < kLevelBatch; ++b, ++L) {
-            if (L + 2 >= g->lvl_cap) {
-                g_err = "basin depth exceeds the site count";
-                return FL_ERR_DEVICE_LIMIT;
-            }
-            FL_LAUNCH(g, kcLevels, 0.0,
-                      k_levels_expand<<<grid, kThreads, 0, g->stream>>>(
-                          L, g->n, g->d_row, g->d_col, g->d_next, g->d_order, g->d_bas,
-                          g->d_lvl, g->d_tail, g->d_flags));
-            FL_LAUNCH(g, kcLevels, 0.0,
-                      k_levels_close<<<1, 1, 0, g->stream>>>(L, g->d_lvl, g->d_tail));
-        }
-        FL_CU(cudaGetLastError());
-        // offsets of the last two levels written: lvl[L] .. lvl[L+1]
-        uint32_t off[2];
-        FL_CU(cudaMemcpyAsync(off, g->d_lvl + L, 8, cudaMemcpyDeviceToHost, g->stream));
-        FL_CU(cudaStreamSynchronize(g->stream));
-        if (off[1] == off[0]) break;   // level L is empty
+    g->stamp = g->stamp == 0x7ffffff0 ? 1 : g->stamp + 1;
+    if (g->stamp == 1) {   // stamps wrapped (or first pass): clear hand-off words
+        FL_CU(cudaMemsetAsync(g->d_bu_done, 0, g->n * 4ull, g->stream));
+        FL_CU(cudaMemsetAsync(g->d_td_need, 0, g->n * 4ull, g->stream));
+        FL_CU(cudaMemsetAsync(g->d_td_done, 0, g->n * 4ull, g->stream));
     }
-    // count non-empty levels
-    std::vector<uint32_t> off(L + 2);
-    FL_CU(cudaMemcpyAsync(off.data(), g->d_lvl, (L + 2) * 4ull, cudaMemcpyDeviceToHost, g->stream));
-    FL_CU(cudaStreamSynchronize(g->stream));
-    uint32_t nl = 0;
-    while (nl < L + 1 && off[nl + 1] > off[nl]) ++nl;
-    *n_levels = nl;
-    // order 4+4, bas 4+4, row_ptr 8 per site; col 4 + next 4 per slot
-    g->k_bytes[kcLevels] += 24.0 * g->n + 8.0 * g->nnz;
-    int h[kNumFlags];
-    FL_TRY(read_flags(g, h));
-    if (h[kError] || off[L] > g->n) {
-        g_err = "basin traversal visited more sites than exist";
-        return FL_ERR_DEVICE_LIMIT;
+    fl::BasinArgs a{};
+    a.n = g->n;
+    a.row = g->d_row;
+    a.col = g->d_col;
+    a.area = g->d_area;
+    a.next = g->d_next;
+    a.rlen = g->d_rlen;
+    a.k = g->d_k;
+    a.u = g->d_u;
+    a.tanms = g->d_tan;
+    a.outlet = g->d_outlet;
+    a.A = g->d_A;
+    a.t = g->d_t;
+    a.w = g->d_w;
+    a.elev = g->d_elev;
+    a.bas = g->d_bas;
+    a.pending = g->d_pending;
+    a.hgt = g->d_hgt;
+    a.order = g->d_order;
+    a.roff = g->d_roff;
+    a.max_rounds = g->max_rounds;
+    a.kahn_min_width = g->kahn_min_width;
+    a.meta = g->d_meta;
+    a.flags = g->d_flags;
+    a.sid = g->d_sid;
+    a.slist = g->d_slist;
+    a.desig = g->d_desig;
+    a.sptr0 = g->d_sptr0;
+    a.sdist0 = g->d_sdist0;
+    a.sptr1 = g->d_sptr1;
+    a.sdist1 = g->d_sdist1;
+    a.cid = g->d_cid;
+    a.cbot = g->d_cbot;
+    a.clen = g->d_clen;
+    a.coff = g->d_coff;
+    a.layout = g->d_layout;
+    a.pre = g->d_pre;
+    a.post = g->d_post;
+    a.sflag = g->d_sflag;
+    a.bu_done = g->d_bu_done;
+    a.td_need = g->d_td_need;
+    a.td_done = g->d_td_done;
+    a.stamp = g->stamp;
+    fl::Hooks hk{g, kbegin, kend};
+    cudaError_t e = fl::basin_pass(a, g->stream, hk, (uint32_t)std::min<uint64_t>(g->nnz, 0xffffffffu));
+    if (e != cudaSuccess) {
+        set_err("basin pass launch", e);
+        return e == cudaErrorMemoryAllocation ? FL_ERR_OUT_OF_MEMORY : FL_ERR_CUDA;
     }
-    return FL_OK;
-}
-
-// Drainage areas, response times, elevations on final receivers.
-int run_tree_pass(fl_graph* g, uint32_t n_out, int* changed) {
-    uint32_t nl = 0;
-    FL_TRY(run_levels(g, n_out, &nl));
-    unsigned grid = 152 * 4;
-    // per-level bytes are not known on the host; the pass total is added to the
-    // last launch: order 4 + row_ptr 8 + area 8 + A 8+8 per site, col 4 + next 4 per slot
-    for (uint32_t L = nl; L-- > 0;)
-        FL_LAUNCH(g, kcArea, L == 0 ? 36.0 * g->n + 8.0 * g->nnz : 0.0,
-                  k_area_level<<<grid, kThreads, 0, g->stream>>>(L, g->d_row, g->d_col,
-                                                                  g->d_next, g->d_order,
-                                                                  g->d_lvl, g->d_area, g->d_A));
-    FL_CU(cudaGetLastError());
-    FL_TRY(clear_flags(g));
-    // order 4, next 4, rlen 8, bas 4, A 8, k 8, u 8, tan 8, t 8+8, t_o 8, e_o 8, e 8+8 per site
-    for (uint32_t L = 0; L < nl; ++L)
-        FL_LAUNCH(g, kcTimeElev, L + 1 == nl ? 112.0 * g->n : 0.0,
-                  k_time_elev_level<<<grid, kThreads, 0, g->stream>>>(
-                      L, g->d_next, g->d_order, g->d_lvl, g->d_bas, g->d_A, g->d_rlen, g->d_k,
-                      g->d_u, g->d_tan, g->d_t, g->d_elev, g->d_flags));
     FL_CU(cudaGetLastError());
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
+    FL_TRY(device_error(h));
     *changed = h[kChanged];
     return FL_OK;
 }
@@ -730,9 +613,15 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     std::vector<uint32_t> outlets = resolve_outlets(g, is_outlet);
     FL_TRY(upload_params(g, base, k, u, max_slope));
     FL_TRY(set_outlets(g, outlets, false));
+    // all status words, including the grid barrier's, start from zero
+    FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
     FL_LAUNCH(g, kcNoise, 16.0 * n,
               k_initial_elevation<<<blocks_for((n + 7) / 8), kThreads, 0, g->stream>>>(
                   n, g->d_base, g->d_elev));
+    // previous-iteration drainage areas steer the skeleton's chain choice; start from
+    // the cell areas
+    FL_LAUNCH(g, kcMisc, 16.0 * n,
+              k_fill_f64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_A, g->d_area));
     FL_CU(cudaGetLastError());
     FL_CU(cudaEventRecord(g->ev0, g->stream));
     if (max_iter > 0xffffffffll) max_iter = 0xffffffffll;
@@ -747,7 +636,7 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
             FL_TRY(run_labels(g));
             FL_TRY(run_lakes(g));
         }
-        FL_TRY(run_tree_pass(g, (uint32_t)outlets.size(), &changed));
+        FL_TRY(run_basin_pass(g, &changed));
         if (!changed) break;
     }
     FL_CU(cudaEventRecord(g->ev1, g->stream));
@@ -874,6 +763,7 @@ int fl_probe_lakes(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     uint32_t n = g->n;
     std::vector<uint32_t> o(outlets, outlets + n_outlets);
     FL_TRY(set_outlets(g, o, true));
+    FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
     FL_CU(cudaMemcpyAsync(g->d_next, next_in, n * 4ull, cudaMemcpyHostToDevice, g->stream));
     std::vector<double> ones(n, 1.0);
     FL_CU(cudaMemcpyAsync(g->d_rlen, ones.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
@@ -910,8 +800,9 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     FL_CU(cudaMemcpyAsync(g->d_rlen, rl.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
     k_fill_f64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_A, g->d_area);
     k_fill_f64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_t, nullptr);
+    FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
     int ch = 0;
-    FL_TRY(run_tree_pass(g, n_outlets, &ch));
+    FL_TRY(run_basin_pass(g, &ch));
     FL_CU(cudaMemcpyAsync(elev, g->d_elev, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
     if (drainage_out) FL_CU(cudaMemcpyAsync(drainage_out, g->d_A, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
     if (response_out) FL_CU(cudaMemcpyAsync(response_out, g->d_t, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
