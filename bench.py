@@ -230,6 +230,7 @@ def bench_gpu(args, d):
     d.barrier()
     _lib.check(L.fl_graph_set_timing(h, 0))
     stats = _lib.kernel_stats(h)
+    basin = _lib.basin_stats(h)
 
     site_iters = d.sum(n * iters)
     loop_max = d.max(loop_ms)
@@ -277,6 +278,7 @@ def bench_gpu(args, d):
         "cpu_baseline": cpu,
         "gpu_launches": launches,
         "kernel_time_share": share,
+        "basin_last_iteration": basin,
         "clocks": clocks.summary(),
         "wall_ms_timed": wall_ms,
     }

@@ -29,6 +29,7 @@ EXPORTS = [
     "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
+    "fl_graph_basin_stats",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
     "fl_probe_rng_f64", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
 ]
@@ -69,6 +70,7 @@ def lib():
     L.fl_graph_reset_stats.restype = None
     L.fl_num_kernel_classes.restype = c_u32
     L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
+    L.fl_graph_basin_stats.argtypes = [vp, vp, c_u32]
     L.fl_probe_receivers.argtypes = [vp, vp, vp, vp, P(c_int)]
     L.fl_probe_lakes.argtypes = [vp, vp, c_u32, vp, vp, vp]
     L.fl_probe_tree_pass.argtypes = [vp, vp, c_u32, vp, vp, vp, vp, vp, vp, vp, P(c_int)]
@@ -127,3 +129,14 @@ def kernel_stats(handle):
                                       ctypes.byref(b)))
         out[name.value.decode()] = (n.value, ms.value, b.value)
     return out
+
+
+BASIN_STATS = ["kahn_rounds", "leaves", "skeleton_sites", "chains", "longest_chain", "slow_sites",
+               "wait_spins_up", "wait_spins_down"]
+
+
+def basin_stats(handle):
+    """Shape of the last basin pass of a model handle."""
+    out = np.zeros(len(BASIN_STATS), np.uint64)
+    check(lib().fl_graph_basin_stats(handle, out.ctypes.data_as(vp), len(BASIN_STATS)))
+    return dict(zip(BASIN_STATS, (int(x) for x in out)))

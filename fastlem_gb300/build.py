@@ -22,7 +22,7 @@ LIB = os.path.join(OUT_DIR, "libfastlem_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_SOURCES = ["solver.cu", "receivers.cu", "basin.cu"]
-CXX_SOURCES = ["builder.cpp", "prim_rank.cpp"]
+CXX_SOURCES = ["builder.cpp", "prim_rank.cpp", "ordering.cpp"]
 HEADERS = ["rng.h", "common.cuh", "kernels.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

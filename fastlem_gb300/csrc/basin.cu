@@ -42,8 +42,9 @@ namespace {
 
 // per-slot flags of the skeleton layout
 constexpr uint8_t kLeafSlot = 1;   // chain leaf: pre holds the complete area
-constexpr uint8_t kHasPost = 2;    // one addition after the chain predecessor
-constexpr uint8_t kSlow = 4;       // confluence or several post additions: full pull at walk time
+constexpr uint8_t kSlow = 4;       // confluence or > kMaxPost additions: full pull at walk time
+constexpr int kPostShift = 3;      // bits 3-4: additions after the chain predecessor (0..3)
+constexpr int kMaxPost = 3;
 
 __device__ __forceinline__ double pull_area(uint32_t v, const uint32_t* __restrict__ row,
                                             const uint32_t* __restrict__ col,
@@ -95,7 +96,8 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
         if (gtid == 0) meta[kMetaCnt0 + ((r + 1) % 3)] = 0;
         for (uint32_t idx = beg + gtid; idx < end; idx += stride) {
             uint32_t v = __ldcg(&order[idx]);
-            A[v] = pull_area(v, row, col, next, area, A);
+            // round 0 is the leaves: no donors, the drainage area is the cell area
+            A[v] = (r == 0) ? area[v] : pull_area(v, row, col, next, area, A);
             hgt[v] = r;
             uint32_t p = next[v];
             if (p != v && atomicSub(&pending[p], 1u) == 1u) {
@@ -232,7 +234,7 @@ __global__ void k_s_bottoms(const uint32_t* __restrict__ slist, Ranks rk,
 // Chain lengths from the skeleton leaves (the final Kahn frontier).
 __global__ void k_s_lengths(const uint32_t* __restrict__ order, const uint32_t* __restrict__ sid,
                             Ranks rk, const uint32_t* __restrict__ cid, uint32_t* __restrict__ clen,
-                            uint32_t max_chains, const uint32_t* meta, const int* flags) {
+                            uint32_t max_chains, uint32_t* meta, const int* flags) {
     if (flags[kError]) return;
     uint32_t b = meta[kMetaFrontBeg], e = meta[kMetaFrontEnd];
     const uint32_t* ptr = rk.P(meta);
@@ -241,6 +243,7 @@ __global__ void k_s_lengths(const uint32_t* __restrict__ order, const uint32_t* 
         uint32_t k = sid[order[i]];
         uint32_t c = cid[ptr[k]];
         if (c < max_chains) clen[c] = dist[k] + 1;
+        atomicMax(&meta[kMetaMaxChain], dist[k] + 1);
     }
 }
 
@@ -271,15 +274,21 @@ __global__ void k_s_scan(const uint32_t* __restrict__ clen, uint32_t* __restrict
 
 __global__ void k_s_layout(const uint32_t* __restrict__ slist, Ranks rk,
                            const uint32_t* __restrict__ cid, const uint32_t* __restrict__ coff,
-                           uint32_t* __restrict__ layout, const uint32_t* meta, int* flags) {
+                           uint32_t* __restrict__ layout, uint32_t* __restrict__ slot_chain,
+                           const uint32_t* meta, int* flags) {
     if (flags[kError]) return;
     uint32_t ns = meta[kMetaNs];
     const uint32_t* ptr = rk.P(meta);
     const uint32_t* dist = rk.D(meta);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
-        uint32_t q = coff[cid[ptr[k]]] + dist[k];
-        if (q < ns) layout[q] = slist[k];
-        else set_error(flags, kErrForest);
+        uint32_t c = cid[ptr[k]];
+        uint32_t q = coff[c] + dist[k];
+        if (q < ns) {
+            layout[q] = slist[k];
+            slot_chain[q] = c;
+        } else {
+            set_error(flags, kErrForest);
+        }
     }
 }
 
@@ -290,16 +299,16 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
                             const uint32_t* __restrict__ col,
                             const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
                             const double* __restrict__ area, const double* __restrict__ A,
-                            const uint32_t* __restrict__ layout, const uint32_t* __restrict__ sid,
-                            Ranks rk, const uint32_t* __restrict__ cid,
+                            const uint32_t* __restrict__ layout,
+                            const uint32_t* __restrict__ slot_chain,
                             const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
                             const uint32_t* __restrict__ cbot, double* __restrict__ pre,
-                            double* __restrict__ post, uint8_t* __restrict__ sflag,
-                            int* __restrict__ td_need, int stamp, const uint32_t* meta,
+                            double* __restrict__ post, double* __restrict__ post1,
+                            double* __restrict__ post2, uint8_t* __restrict__ sflag,
+                            int* __restrict__ td_need, int stamp, uint32_t* meta,
                             int* flags) {
     if (flags[kError]) return;
     uint32_t ns = meta[kMetaNs];
-    const uint32_t* ptr = rk.P(meta);
     uint32_t nc = meta[kMetaChains];
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x) {
         uint32_t v = layout[q];
@@ -307,13 +316,16 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
             set_error(flags, kErrForest);
             return;
         }
-        uint32_t c = cid[ptr[sid[v]]];
+        uint32_t c = slot_chain[q];
         uint32_t last = coff[c] + clen[c] - 1;
         uint32_t heavy = q < last ? layout[q + 1] : kNone;
         double a = area[v];
-        double ps = 0.0;
+        double ps[kMaxPost] = {0.0, 0.0, 0.0};
+        int np = 0;
         uint8_t f = (q == last) ? kLeafSlot : 0;
         bool seen_heavy = false;
+        // reverse row order: additions before the predecessor fold into pre, the ones
+        // after it are replayed by the walk
         for (uint32_t s = row[v + 1]; s-- > row[v];) {
             uint32_t d = col[s];
             if (d == v || next[d] != v) continue;
@@ -328,17 +340,19 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
             double val = A[d];
             if (!seen_heavy) {
                 a = __dadd_rn(a, val);
-            } else if (!(f & kHasPost)) {
-                ps = val;
-                f |= kHasPost;
+            } else if (np < kMaxPost) {
+                ps[np++] = val;
             } else {
                 f |= kSlow;
                 break;
             }
         }
         pre[q] = a;
-        post[q] = ps;
-        sflag[q] = f;
+        post[q] = ps[0];
+        post1[q] = ps[1];
+        post2[q] = ps[2];
+        sflag[q] = f | (uint8_t)(np << kPostShift);
+        if (f & kSlow) atomicAdd(&meta[kMetaSlow], 1u);
     }
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         uint32_t b = cbot[c];
@@ -352,7 +366,8 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
 __device__ double slow_pull(uint32_t v, uint32_t heavy, double x, const uint32_t* __restrict__ row,
                             const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
                             const uint32_t* __restrict__ hgt, const double* __restrict__ area,
-                            const double* A, const int* bu_done, int stamp, int* flags, bool* ok) {
+                            const double* A, const int* bu_done, int stamp, int* flags, bool* ok,
+                            uint32_t* spin_total) {
     double a = area[v];
     for (uint32_t s = row[v + 1]; s-- > row[v];) {
         uint32_t d = col[s];
@@ -371,6 +386,7 @@ __device__ double slow_pull(uint32_t v, uint32_t heavy, double x, const uint32_t
                     }
                     __nanosleep(32);
                 }
+                *spin_total += spins;
             }
             val = __ldcg(&A[d]);
         }
@@ -379,42 +395,112 @@ __device__ double slow_pull(uint32_t v, uint32_t heavy, double x, const uint32_t
     return a;
 }
 
+constexpr int kBatch = 8;
+
+// One thread per chain, leaf to bottom.  Operands are read in layout order in
+// batches of kBatch, the next batch's loads issued before the current batch's
+// dependent additions.  Results go to Al (layout order); the chain bottom's area
+// is also stored in A and published through bu_done.
 __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
                               const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
                               const double* __restrict__ area, double* A,
                               const uint32_t* __restrict__ layout,
                               const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
                               const double* __restrict__ pre, const double* __restrict__ post,
-                              const uint8_t* __restrict__ sflag, int* bu_done, int stamp,
-                              const uint32_t* meta, int* flags) {
+                              const double* __restrict__ post1, const double* __restrict__ post2,
+                              const uint8_t* __restrict__ sflag, double* __restrict__ Al,
+                              int* bu_done, int stamp, uint32_t* meta, int* flags) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= meta[kMetaChains] || flags[kError]) return;
     const uint32_t off = coff[c];
-    uint32_t q = off + clen[c];
-    if (q > meta[kMetaNs] || q == off) {
+    const uint32_t len = clen[c];
+    if (off + len > meta[kMetaNs] || len == 0) {
         set_error(flags, kErrForest);
         return;
     }
     double x = 0.0;
-    uint32_t prev = kNone;
     bool ok = true;
-    while (q-- > off) {
-        const uint32_t v = layout[q];
-        const uint8_t f = sflag[q];
-        if (f & kLeafSlot) {
-            x = pre[q];
-        } else if (!(f & kSlow)) {
-            x = __dadd_rn(pre[q], x);
-            if (f & kHasPost) x = __dadd_rn(x, post[q]);
-        } else {
-            x = slow_pull(v, prev, x, row, col, next, hgt, area, A, bu_done, stamp, flags, &ok);
-            if (!ok) return;
+    uint32_t spins = 0;
+    // positions are processed from hi = off + len - 1 down to off
+    int32_t q = (int32_t)(off + len) - 1;
+    double bp[kBatch], bq[kBatch], br[kBatch], bs[kBatch];
+    uint8_t bf[kBatch];
+    auto load = [&](int32_t top, double* P, double* Q, double* R, double* S, uint8_t* F) {
+#pragma unroll
+        for (int i = 0; i < kBatch; ++i) {
+            int32_t qq = top - i;
+            if (qq >= (int32_t)off) {
+                P[i] = pre[qq];
+                Q[i] = post[qq];
+                R[i] = post1[qq];
+                S[i] = post2[qq];
+                F[i] = sflag[qq];
+            }
         }
-        A[v] = x;
-        prev = v;
+    };
+    load(q, bp, bq, br, bs, bf);
+    while (q >= (int32_t)off) {
+        double np[kBatch], nq[kBatch], nr[kBatch], ns[kBatch];
+        uint8_t nf[kBatch];
+        load(q - kBatch, np, nq, nr, ns, nf);    // next batch in flight
+#pragma unroll
+        for (int i = 0; i < kBatch; ++i) {
+            int32_t qq = q - i;
+            if (qq < (int32_t)off) break;
+            uint8_t f = bf[i];
+            if (f & kLeafSlot) {
+                x = bp[i];
+            } else if (!(f & kSlow)) {
+                int npost = (f >> kPostShift) & 3;
+                x = __dadd_rn(bp[i], x);
+                if (npost > 0) x = __dadd_rn(x, bq[i]);
+                if (npost > 1) x = __dadd_rn(x, br[i]);
+                if (npost > 2) x = __dadd_rn(x, bs[i]);
+            } else {
+                x = slow_pull(layout[qq], layout[qq + 1], x, row, col, next, hgt, area, A, bu_done,
+                              stamp, flags, &ok, &spins);
+                if (!ok) return;
+            }
+            Al[qq] = x;
+        }
+        q -= kBatch;
+#pragma unroll
+        for (int i = 0; i < kBatch; ++i) {
+            bp[i] = np[i];
+            bq[i] = nq[i];
+            br[i] = nr[i];
+            bs[i] = ns[i];
+            bf[i] = nf[i];
+        }
     }
+    uint32_t bottom = layout[off];
+    A[bottom] = x;
     __threadfence();
-    st_release(&bu_done[prev], stamp);
+    st_release(&bu_done[bottom], stamp);
+    if (spins) atomicAdd(&meta[kMetaSpinUp], spins);
+}
+
+// Skeleton areas back to site order.
+__global__ void k_s_scatter(const uint32_t* __restrict__ layout, const double* __restrict__ src,
+                            double* __restrict__ dst, const uint32_t* meta, const int* flags) {
+    if (flags[kError]) return;
+    uint32_t ns = meta[kMetaNs];
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x)
+        dst[layout[q]] = src[q];
+}
+
+// Top-down operands in layout order: w, and whether another chain waits for the site.
+__global__ void k_s_gather_down(const uint32_t* __restrict__ layout, const double* __restrict__ w,
+                                const int* __restrict__ td_need, int stamp,
+                                double* __restrict__ wl, uint8_t* __restrict__ needl,
+                                const uint32_t* meta, const int* flags) {
+    if (flags[kError]) return;
+    uint32_t ns = meta[kMetaNs];
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x) {
+        uint32_t v = layout[q];
+        wl[q] = w[v];
+        needl[q] = td_need[v] == stamp ? 1 : 0;
+    }
 }
 
 // w_v = (1 / (k_v * sqrt(A_v))) * len_v  (generator.rs:172-173)
@@ -474,22 +560,45 @@ __device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t
     return tv;
 }
 
+// One thread per chain, bottom to leaf: t_v = 0 + (t_parent + w_v).  Without slope
+// limits only t is carried (tl, layout order; elevations follow in k_s_finish); with
+// them the elevation and its clamp against the receiver are carried too.  The chain's
+// basin outlet and its t / elevation are stored per chain.  Sites another chain
+// waits for are written to t / elev / bas directly and published through td_done.
 __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
                              const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
-                             const int* __restrict__ td_need, int* td_done, int stamp,
-                             const uint32_t* meta) {
+                             const double* __restrict__ wl, const uint8_t* __restrict__ needl,
+                             double* __restrict__ tl, double* __restrict__ el,
+                             uint32_t* __restrict__ cbas, double* __restrict__ cto,
+                             double* __restrict__ ceo, bool slope, int* td_done, int stamp,
+                             uint32_t* meta) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= meta[kMetaChains] || td.flags[kError]) return;
-    const uint32_t off = coff[c], end = off + clen[c];
-    if (end > meta[kMetaNs] || end == off) {
+    const uint32_t off = coff[c], len = clen[c];
+    if (off + len > meta[kMetaNs] || len == 0) {
         set_error(td.flags, kErrForest);
         return;
     }
     uint32_t v = layout[off];
     uint32_t p = td.next[v];
-    double tp = 0.0, ep = 0.0, to = 0.0, eo = 0.0;
+    double tp, ep, to = 0.0, eo = 0.0;
     uint32_t o = kNone;
-    if (p != v) {
+    uint32_t q = off;
+    if (p == v) {                         // the chain starts at a root
+        double e;
+        tp = settle(td, v, p, 0.0, kNone, 0.0, 0.0, 0.0, &e);
+        ep = e;
+        o = td.outlet[v] ? v : kNone;
+        to = tp;
+        eo = e;
+        tl[q] = tp;
+        if (slope) el[q] = e;
+        if (needl[q]) {
+            __threadfence();
+            st_release(&td_done[v], stamp);
+        }
+        ++q;
+    } else {
         uint32_t spins = 0;
         while (ld_acquire(&td_done[p]) != stamp) {
             if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
@@ -498,6 +607,7 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
             }
             __nanosleep(32);
         }
+        if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
         tp = __ldcg(&td.t[p]);
         ep = __ldcg(&td.elev[p]);
         o = __ldcg(&td.bas[p]);
@@ -506,22 +616,101 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
             eo = __ldcg(&td.elev[o]);
         }
     }
-    for (uint32_t q = off; q < end; ++q) {
-        v = layout[q];
-        double e;
-        double tv = settle(td, v, p, tp, o, to, eo, ep, &e);
-        if (p == v) {                     // chain bottom is a root
-            o = td.outlet[v] ? v : kNone;
-            to = tv;
-            eo = e;
+    cbas[c] = o;
+    cto[c] = to;
+    ceo[c] = eo;
+    const uint32_t end = off + len;
+    if (!slope) {
+        double bw[kBatch];
+        uint8_t bn[kBatch];
+#pragma unroll
+        for (int i = 0; i < kBatch; ++i) {
+            if (q + i < end) {
+                bw[i] = wl[q + i];
+                bn[i] = needl[q + i];
+            }
         }
-        if (td_need[v] == stamp) {
-            __threadfence();
-            st_release(&td_done[v], stamp);
+        while (q < end) {
+            double nw[kBatch];
+            uint8_t nn[kBatch];
+#pragma unroll
+            for (int i = 0; i < kBatch; ++i) {
+                if (q + kBatch + i < end) {
+                    nw[i] = wl[q + kBatch + i];
+                    nn[i] = needl[q + kBatch + i];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < kBatch; ++i) {
+                if (q + i >= end) break;
+                tp = plus_zero(__dadd_rn(tp, bw[i]));
+                tl[q + i] = tp;
+                if (bn[i]) {                   // another chain hangs here: publish t, elev, bas
+                    uint32_t u = layout[q + i];
+                    double e = __ldcg(&td.elev[u]);
+                    if (o != kNone) {
+                        double dt = __dsub_rn(tp, to);
+                        e = __dadd_rn(eo, __dmul_rn(td.uu[u], dt > 0.0 ? dt : 0.0));
+                        if (e != __ldcg(&td.elev[u])) td.flags[kChanged] = 1;
+                    }
+                    td.t[u] = tp;
+                    td.elev[u] = e;
+                    td.bas[u] = o;
+                    __threadfence();
+                    st_release(&td_done[u], stamp);
+                }
+            }
+            q += kBatch;
+#pragma unroll
+            for (int i = 0; i < kBatch; ++i) {
+                bw[i] = nw[i];
+                bn[i] = nn[i];
+            }
         }
-        tp = tv;
-        ep = e;
-        p = v;
+    } else {
+        for (; q < end; ++q) {
+            v = layout[q];
+            double e;
+            tp = settle(td, v, p, tp, o, to, eo, ep, &e);
+            tl[q] = tp;
+            el[q] = e;
+            ep = e;
+            p = v;
+            if (needl[q]) {
+                __threadfence();
+                st_release(&td_done[v], stamp);
+            }
+        }
+    }
+}
+
+// Skeleton response times and elevations back to site order.
+__global__ void k_s_finish(TopDown td, const uint32_t* __restrict__ layout,
+                           const uint32_t* __restrict__ slot_chain, const double* __restrict__ tl,
+                           const double* __restrict__ el, const uint32_t* __restrict__ cbas,
+                           const double* __restrict__ cto, const double* __restrict__ ceo,
+                           bool slope, const uint32_t* meta) {
+    if (td.flags[kError]) return;
+    uint32_t ns = meta[kMetaNs];
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x) {
+        uint32_t v = layout[q];
+        if (td.next[v] == v) continue;     // roots were settled by the walker
+        uint32_t c = slot_chain[q];
+        uint32_t o = cbas[c];
+        double tv = tl[q];
+        td.t[v] = tv;
+        td.bas[v] = o;
+        if (o == kNone) continue;
+        double old_e = td.elev[v];
+        double ne;
+        if (slope) {
+            ne = el[q];
+        } else {
+            double dt = __dsub_rn(tv, cto[c]);
+            ne = __dadd_rn(ceo[c], __dmul_rn(td.uu[v], dt > 0.0 ? dt : 0.0));
+        }
+        if (ne != old_e) td.flags[kChanged] = 1;
+        td.elev[v] = ne;
     }
 }
 
@@ -576,9 +765,9 @@ unsigned coop_grid(const void* kernel, unsigned cap_per_sm) {
 cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz) {
     const uint32_t n = a.n;
     const unsigned nb = (n + kThreads - 1) / kThreads;
-    const unsigned g_kahn = coop_grid((const void*)k_kahn, 4);
-    const unsigned g_rank = coop_grid((const void*)k_s_rank, 4);
-    const unsigned g_low = coop_grid((const void*)k_low_top_down, 4);
+    const unsigned g_kahn = coop_grid((const void*)k_kahn, 8);
+    const unsigned g_rank = coop_grid((const void*)k_s_rank, 8);
+    const unsigned g_low = coop_grid((const void*)k_low_top_down, 8);
     const unsigned g_chain = (a.kahn_min_width + kThreads - 1) / kThreads;
     const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
@@ -621,20 +810,27 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     k_s_lengths<<<gs, kThreads, 0, st>>>(a.order, a.sid, rk, a.cid, a.clen, a.kahn_min_width, a.meta,
                                          a.flags);
     k_s_scan<<<1, 1024, 0, st>>>(a.clen, a.coff, a.meta, a.flags);
-    k_s_layout<<<gs, kThreads, 0, st>>>(a.slist, rk, a.cid, a.coff, a.layout, a.meta, a.flags);
+    k_s_layout<<<gs, kThreads, 0, st>>>(a.slist, rk, a.cid, a.coff, a.layout, a.slot_chain, a.meta,
+                                        a.flags);
     k_s_prepare<<<gs, kThreads, 0, st>>>(n, a.row, a.col, a.next, a.hgt, a.area, a.A, a.layout,
-                                         a.sid, rk, a.cid, a.coff, a.clen, a.cbot, a.pre, a.post,
-                                         a.sflag, a.td_need, a.stamp, a.meta, a.flags);
+                                         a.slot_chain, a.coff, a.clen, a.cbot, a.pre, a.post,
+                                         a.post1, a.post2, a.sflag, a.td_need, a.stamp, a.meta,
+                                         a.flags);
     hk.end(hk.ctx, kcBasinBuild, 0.0);
 
+    // chain walk bottom-up; results in layout order (in place over `pre`)
     hk.begin(hk.ctx);
     e = coop_launch(k_s_bottom_up, g_chain, kThreads, st, a.row, a.col, a.next,
                     (const uint32_t*)a.hgt, a.area, a.A, (const uint32_t*)a.layout,
                     (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const double*)a.pre,
-                    (const double*)a.post, (const uint8_t*)a.sflag, a.bu_done, a.stamp,
-                    (const uint32_t*)a.meta, a.flags);
+                    (const double*)a.post, (const double*)a.post1, (const double*)a.post2,
+                    (const uint8_t*)a.sflag, a.pre, a.bu_done, a.stamp, a.meta, a.flags);
     hk.end(hk.ctx, kcSkelUp, 0.0);
     if (e != cudaSuccess) return e;
+
+    hk.begin(hk.ctx);
+    k_s_scatter<<<gs, kThreads, 0, st>>>(a.layout, a.pre, a.A, a.meta, a.flags);
+    hk.end(hk.ctx, kcBasinBuild, 0.0);
 
     // w: A 8 + k 8 + rlen 8 + w 8 per site
     hk.begin(hk.ctx);
@@ -642,11 +838,25 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     hk.end(hk.ctx, kcW, 32.0 * n);
 
     hk.begin(hk.ctx);
+    k_s_gather_down<<<gs, kThreads, 0, st>>>(a.layout, a.w, a.td_need, a.stamp, a.post, a.sflag,
+                                             a.meta, a.flags);
+    hk.end(hk.ctx, kcBasinBuild, 0.0);
+
+    hk.begin(hk.ctx);
     e = coop_launch(k_s_top_down, g_chain, kThreads, st, td, (const uint32_t*)a.layout,
-                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const int*)a.td_need,
-                    a.td_done, a.stamp, (const uint32_t*)a.meta);
+                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const double*)a.post,
+                    (const uint8_t*)a.sflag, a.pre, a.el, a.cbas, a.cto, a.ceo, a.slope,
+                    a.td_done, a.stamp, a.meta);
     hk.end(hk.ctx, kcSkelDown, 0.0);
     if (e != cudaSuccess) return e;
+
+    hk.begin(hk.ctx);
+    k_s_finish<<<gs, kThreads, 0, st>>>(td, (const uint32_t*)a.layout,
+                                        (const uint32_t*)a.slot_chain, (const double*)a.pre,
+                                        (const double*)a.el, (const uint32_t*)a.cbas,
+                                        (const double*)a.cto, (const double*)a.ceo, a.slope,
+                                        (const uint32_t*)a.meta);
+    hk.end(hk.ctx, kcBasinBuild, 0.0);
 
     // top-down rounds: order 4, next 4, w 8, u 8, tan 8, rlen 8, elev 8+8, t 8, bas 4,
     // parent t/elev/bas 20, outlet t/elev 16 per site

@@ -36,6 +36,10 @@ enum Meta {
     kMetaJump2,
     kMetaRankBuf,      // which ping-pong buffer holds the ranks
     kMetaChains,       // number of skeleton chains
+    kMetaSlow,         // skeleton sites needing the full pull at walk time
+    kMetaSpinUp,       // wait iterations of the bottom-up chain hand-offs
+    kMetaSpinDown,     // wait iterations of the top-down chain hand-offs
+    kMetaMaxChain,     // longest skeleton chain
     kMetaCount
 };
 
@@ -76,8 +80,16 @@ struct BasinArgs {
     uint32_t* clen;
     uint32_t* coff;
     uint32_t* layout;
+    uint32_t* slot_chain;   // layout slot -> chain
+    double* el;             // skeleton elevations in layout order (slope limits only)
+    uint32_t* cbas;         // per chain: basin outlet, its response time and elevation
+    double* cto;
+    double* ceo;
+    bool slope;             // some site has a maximum slope
     double* pre;
     double* post;
+    double* post1;
+    double* post2;
     uint8_t* sflag;
     int* bu_done;
     int* td_need;

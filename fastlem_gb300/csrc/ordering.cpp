@@ -1,0 +1,90 @@
+// ordering.cpp -- device memory order of a model's sites.
+//
+// Synthetic and builder-made sites come in random order, so a site's neighbours,
+// receiver and donors are scattered over the whole array and every gather misses
+// the caches.  The solver therefore stores sites in the order of a Hilbert curve
+// through the bounding box of their coordinates: neighbours and river paths land on
+// nearby indices.  Relabelling never changes results: every row keeps its slot
+// order (the adjacency order the reference's tie-breaks and sums follow), outlet
+// lists keep their order, and all inputs / outputs are translated at the boundary.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+namespace fl {
+
+// Position of grid cell (x, y) along the Hilbert curve filling a 2^order square
+// (the classic quadrant-rotation construction).
+static uint64_t hilbert_index(uint32_t order, uint32_t x, uint32_t y) {
+    uint64_t d = 0;
+    for (uint32_t s = 1u << (order - 1); s > 0; s >>= 1) {
+        uint32_t rx = (x & s) ? 1u : 0u;
+        uint32_t ry = (y & s) ? 1u : 0u;
+        d += (uint64_t)s * s * ((3u * rx) ^ ry);
+        if (ry == 0) {
+            if (rx == 1) {
+                x = s - 1 - (x & (s - 1)) + (x & ~(s - 1));
+                y = s - 1 - (y & (s - 1)) + (y & ~(s - 1));
+            }
+            uint32_t t = x;
+            x = y;
+            y = t;
+        }
+    }
+    return d;
+}
+
+// perm[new] = old for the Hilbert order of (xs, ys); ties keep index order.
+void hilbert_order(uint32_t n, const double* xs, const double* ys, std::vector<uint32_t>& perm) {
+    double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (std::isfinite(xs[i])) { x0 = std::min(x0, xs[i]); x1 = std::max(x1, xs[i]); }
+        if (std::isfinite(ys[i])) { y0 = std::min(y0, ys[i]); y1 = std::max(y1, ys[i]); }
+    }
+    const uint32_t order = 16;
+    const double cells = (double)((1u << order) - 1);
+    double sx = (x1 > x0) ? cells / (x1 - x0) : 0.0;
+    double sy = (y1 > y0) ? cells / (y1 - y0) : 0.0;
+    std::vector<uint32_t> key(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        double fx = std::isfinite(xs[i]) ? (xs[i] - x0) * sx : 0.0;
+        double fy = std::isfinite(ys[i]) ? (ys[i] - y0) * sy : 0.0;
+        uint32_t cx = (uint32_t)std::min(cells, std::max(0.0, fx));
+        uint32_t cy = (uint32_t)std::min(cells, std::max(0.0, fy));
+        key[i] = (uint32_t)hilbert_index(order, cx, cy);   // < 2^32 for order 16
+    }
+    // stable LSD radix sort of (key, index), 4 passes of 8 bits
+    perm.resize(n);
+    for (uint32_t i = 0; i < n; ++i) perm[i] = i;
+    std::vector<uint32_t> tmp(n);
+    for (int shift = 0; shift < 32; shift += 8) {
+        uint32_t cnt[257] = {0};
+        for (uint32_t i = 0; i < n; ++i) ++cnt[((key[perm[i]] >> shift) & 255u) + 1];
+        for (int b = 0; b < 256; ++b) cnt[b + 1] += cnt[b];
+        for (uint32_t i = 0; i < n; ++i) tmp[cnt[(key[perm[i]] >> shift) & 255u]++] = perm[i];
+        perm.swap(tmp);
+    }
+}
+
+// CSR of the relabelled graph: new row j is old row perm[j] with columns mapped
+// through inv, slot order unchanged.
+void relabel_csr(uint32_t n, const uint32_t* row, const uint32_t* col, const double* len,
+                 const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
+                 std::vector<uint32_t>& nrow, std::vector<uint32_t>& ncol, std::vector<double>& nlen) {
+    nrow.assign(n + 1, 0);
+    for (uint32_t j = 0; j < n; ++j) nrow[j + 1] = nrow[j] + (row[perm[j] + 1] - row[perm[j]]);
+    ncol.resize(nrow[n]);
+    nlen.resize(nrow[n]);
+    for (uint32_t j = 0; j < n; ++j) {
+        uint32_t o = perm[j];
+        uint32_t d = nrow[j];
+        for (uint32_t s = row[o]; s < row[o + 1]; ++s, ++d) {
+            ncol[d] = inv[col[s]];
+            nlen[d] = len[s];
+        }
+    }
+}
+
+}  // namespace fl

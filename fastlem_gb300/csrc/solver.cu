@@ -36,6 +36,10 @@
 namespace fl {
 bool lake_heap_rank(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
                     const uint32_t* outlets, uint32_t n_out, uint32_t* rank);
+void hilbert_order(uint32_t n, const double* xs, const double* ys, std::vector<uint32_t>& perm);
+void relabel_csr(uint32_t n, const uint32_t* row, const uint32_t* col, const double* len,
+                 const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
+                 std::vector<uint32_t>& nrow, std::vector<uint32_t>& ncol, std::vector<double>& nlen);
 }
 
 namespace {
@@ -81,10 +85,9 @@ inline unsigned blocks_for(uint64_t n, int t = kThreads) {
 // Kernels
 // ---------------------------------------------------------------------------
 
-// elev[i] = base[i] + gen::<f64>() * f64::EPSILON, sample i of seed_from_u64(0)
-// (generator.rs:134-138).  One thread per ChaCha block = 8 consecutive sites.
-__global__ void k_initial_elevation(uint32_t n, const double* __restrict__ base,
-                                    double* __restrict__ elev) {
+// noise[i] = sample i of StdRng::seed_from_u64(0).gen::<f64>() (generator.rs:134-137),
+// in the caller's site order.  One thread per ChaCha block = 8 consecutive samples.
+__global__ void k_noise(uint32_t n, double* __restrict__ noise) {
     uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b * 8 >= n) return;
     uint32_t key[8];
@@ -94,11 +97,23 @@ __global__ void k_initial_elevation(uint32_t n, const double* __restrict__ base,
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
         uint64_t i = b * 8 + m;
-        if (i < n) {
-            uint64_t v = (uint64_t)w[2 * m] | ((uint64_t)w[2 * m + 1] << 32);
-            elev[i] = __dadd_rn(base[i], __dmul_rn(fl::u64_to_unit_f64(v), kEpsilon));
-        }
+        if (i < n) noise[i] = fl::u64_to_unit_f64((uint64_t)w[2 * m] | ((uint64_t)w[2 * m + 1] << 32));
     }
+}
+
+// elev[j] = base[j] + noise[perm[j]] * f64::EPSILON (generator.rs:135-138), device order.
+__global__ void k_initial_elevation(uint32_t n, const uint32_t* __restrict__ perm,
+                                    const double* __restrict__ base,
+                                    const double* __restrict__ noise, double* __restrict__ elev) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) elev[j] = __dadd_rn(base[j], __dmul_rn(noise[perm[j]], kEpsilon));
+}
+
+// dst[j] = src[idx[j]]: caller order <-> device order.
+__global__ void k_gather_f64(uint32_t n, const uint32_t* __restrict__ idx,
+                             const double* __restrict__ src, double* __restrict__ dst) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) dst[j] = src[idx[j]];
 }
 
 __global__ void k_rng_f64(uint64_t seed, uint64_t first, uint64_t count, double* out) {
@@ -229,6 +244,9 @@ struct fl_graph {
     bool rank_valid = false;
     bool rank_uploaded = false;
     std::vector<uint32_t> h_rank;
+    // device order: perm[device index] = caller index, inv the reverse
+    std::vector<uint32_t> perm, inv;
+    uint32_t *d_perm = nullptr, *d_inv = nullptr;
     // model (device)
     uint32_t *d_row = nullptr, *d_col = nullptr;
     double *d_len = nullptr, *d_area = nullptr;
@@ -245,12 +263,15 @@ struct fl_graph {
              *d_meta = nullptr, *d_sid = nullptr, *d_slist = nullptr, *d_desig = nullptr,
              *d_sptr0 = nullptr, *d_sdist0 = nullptr, *d_sptr1 = nullptr, *d_sdist1 = nullptr,
              *d_cid = nullptr, *d_cbot = nullptr, *d_clen = nullptr, *d_coff = nullptr,
-             *d_layout = nullptr;
-    double *d_pre = nullptr, *d_post = nullptr;
+             *d_layout = nullptr, *d_slot_chain = nullptr, *d_cbas = nullptr;
+    double *d_pre = nullptr, *d_post = nullptr, *d_post1 = nullptr, *d_post2 = nullptr,
+           *d_el = nullptr, *d_cto = nullptr, *d_ceo = nullptr;
+    bool slope = false;
     uint8_t* d_sflag = nullptr;
     int *d_bu_done = nullptr, *d_td_need = nullptr, *d_td_done = nullptr;
     uint32_t max_rounds = 0, kahn_min_width = kKahnMinWidth;
     int stamp = 0;
+    uint32_t last_meta[kMetaCount] = {};
     // instrumentation: launches / algorithmic bytes always, device time when enabled
     bool timing = false;
     uint64_t k_launches[kcCount] = {};
@@ -277,7 +298,9 @@ void free_graph(fl_graph* g) {
                     g->d_flags, g->d_pending, g->d_hgt, g->d_order, g->d_roff, g->d_meta,
                     g->d_sid, g->d_slist, g->d_desig, g->d_sptr0, g->d_sdist0, g->d_sptr1,
                     g->d_sdist1, g->d_cid, g->d_cbot, g->d_clen, g->d_coff, g->d_layout,
-                    g->d_pre, g->d_post, g->d_sflag, g->d_bu_done, g->d_td_need, g->d_td_done};
+                    g->d_pre, g->d_post, g->d_sflag, g->d_bu_done, g->d_td_need, g->d_td_done,
+                    g->d_slot_chain, g->d_cbas, g->d_el, g->d_cto, g->d_ceo, g->d_perm, g->d_inv,
+                    g->d_post1, g->d_post2};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -381,8 +404,15 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_clen, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_coff, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_layout, n));
+    FL_TRY(dalloc(&g->d_slot_chain, n));
+    FL_TRY(dalloc(&g->d_el, n));
+    FL_TRY(dalloc(&g->d_cbas, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_cto, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_ceo, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_pre, n));
     FL_TRY(dalloc(&g->d_post, n));
+    FL_TRY(dalloc(&g->d_post1, n));
+    FL_TRY(dalloc(&g->d_post2, n));
     FL_TRY(dalloc(&g->d_sflag, n));
     FL_TRY(dalloc(&g->d_bu_done, n));
     FL_TRY(dalloc(&g->d_td_need, n));
@@ -418,12 +448,37 @@ int device_error(const int* h) {
 }
 
 // Outlet list as generate() resolves it (generator.rs:120-132).
+// Returned in device ids, list order unchanged (the order matters to the lake heap).
 std::vector<uint32_t> resolve_outlets(const fl_graph* g, const uint8_t* is_outlet) {
     std::vector<uint32_t> o;
     for (uint32_t i = 0; i < g->n; ++i)
-        if (is_outlet[i]) o.push_back(i);
+        if (is_outlet[i]) o.push_back(g->inv[i]);
     if (o.empty()) o = g->def_outlets;
     return o;
+}
+
+std::vector<uint32_t> to_device_ids(const fl_graph* g, const uint32_t* ids, uint32_t count) {
+    std::vector<uint32_t> o(count);
+    for (uint32_t i = 0; i < count; ++i) o[i] = g->inv[ids[i]];
+    return o;
+}
+
+// Uploads a caller-order f64 array into device order.
+int upload_permuted(fl_graph* g, const double* src, double* dst) {
+    FL_CU(cudaMemcpyAsync(g->d_t, src, g->n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    k_gather_f64<<<blocks_for(g->n), kThreads, 0, g->stream>>>(g->n, g->d_perm, g->d_t, dst);
+    FL_CU(cudaGetLastError());
+    return FL_OK;
+}
+
+// Downloads a device-order f64 array into caller order.
+int download_permuted(fl_graph* g, const double* src, double* dst) {
+    // w is dead after a pass (and response times must survive the downloads)
+    double* stage = (src == g->d_w) ? g->d_t : g->d_w;
+    k_gather_f64<<<blocks_for(g->n), kThreads, 0, g->stream>>>(g->n, g->d_inv, src, stage);
+    FL_CU(cudaGetLastError());
+    FL_CU(cudaMemcpyAsync(dst, stage, g->n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    return FL_OK;
 }
 
 // Uploads the outlet list and table, computing (or reusing) the lake-heap rank.
@@ -563,8 +618,16 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.clen = g->d_clen;
     a.coff = g->d_coff;
     a.layout = g->d_layout;
+    a.slot_chain = g->d_slot_chain;
+    a.el = g->d_el;
+    a.cbas = g->d_cbas;
+    a.cto = g->d_cto;
+    a.ceo = g->d_ceo;
+    a.slope = g->slope;
     a.pre = g->d_pre;
     a.post = g->d_post;
+    a.post1 = g->d_post1;
+    a.post2 = g->d_post2;
     a.sflag = g->d_sflag;
     a.bu_done = g->d_bu_done;
     a.td_need = g->d_td_need;
@@ -577,6 +640,8 @@ int run_basin_pass(fl_graph* g, int* changed) {
         return e == cudaErrorMemoryAllocation ? FL_ERR_OUT_OF_MEMORY : FL_ERR_CUDA;
     }
     FL_CU(cudaGetLastError());
+    FL_CU(cudaMemcpyAsync(g->last_meta, g->d_meta, sizeof g->last_meta, cudaMemcpyDeviceToHost,
+                          g->stream));
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
     FL_TRY(device_error(h));
@@ -588,12 +653,25 @@ int upload_params(fl_graph* g, const double* base, const double* k, const double
                   const double* max_slope) {
     uint32_t n = g->n;
     std::vector<double> tanv(n);
-    for (uint32_t i = 0; i < n; ++i)
+    g->slope = false;
+    for (uint32_t i = 0; i < n; ++i) {
         tanv[i] = (max_slope && !std::isnan(max_slope[i])) ? std::tan(max_slope[i]) : NAN;
-    if (base) FL_CU(cudaMemcpyAsync(g->d_base, base, n * 8ull, cudaMemcpyHostToDevice, g->stream));
-    if (k) FL_CU(cudaMemcpyAsync(g->d_k, k, n * 8ull, cudaMemcpyHostToDevice, g->stream));
-    if (u) FL_CU(cudaMemcpyAsync(g->d_u, u, n * 8ull, cudaMemcpyHostToDevice, g->stream));
-    FL_CU(cudaMemcpyAsync(g->d_tan, tanv.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
+        if (!std::isnan(tanv[i])) g->slope = true;
+    }
+    // one staging buffer: each upload waits for the previous gather to consume it
+    if (base) {
+        FL_TRY(upload_permuted(g, base, g->d_base));
+        FL_CU(cudaStreamSynchronize(g->stream));
+    }
+    if (k) {
+        FL_TRY(upload_permuted(g, k, g->d_k));
+        FL_CU(cudaStreamSynchronize(g->stream));
+    }
+    if (u) {
+        FL_TRY(upload_permuted(g, u, g->d_u));
+        FL_CU(cudaStreamSynchronize(g->stream));
+    }
+    FL_TRY(upload_permuted(g, tanv.data(), g->d_tan));
     FL_CU(cudaStreamSynchronize(g->stream));
     return FL_OK;
 }
@@ -615,9 +693,11 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     FL_TRY(set_outlets(g, outlets, false));
     // all status words, including the grid barrier's, start from zero
     FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
-    FL_LAUNCH(g, kcNoise, 16.0 * n,
-              k_initial_elevation<<<blocks_for((n + 7) / 8), kThreads, 0, g->stream>>>(
-                  n, g->d_base, g->d_elev));
+    FL_LAUNCH(g, kcNoise, 8.0 * n,
+              k_noise<<<blocks_for((n + 7) / 8), kThreads, 0, g->stream>>>(n, g->d_w));
+    FL_LAUNCH(g, kcNoise, 28.0 * n,
+              k_initial_elevation<<<blocks_for(n), kThreads, 0, g->stream>>>(
+                  n, g->d_perm, g->d_base, g->d_w, g->d_elev));
     // previous-iteration drainage areas steer the skeleton's chain choice; start from
     // the cell areas
     FL_LAUNCH(g, kcMisc, 16.0 * n,
@@ -640,7 +720,7 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
         if (!changed) break;
     }
     FL_CU(cudaEventRecord(g->ev1, g->stream));
-    FL_CU(cudaMemcpyAsync(out_elev, g->d_elev, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_TRY(download_permuted(g, g->d_elev, out_elev));
     FL_CU(cudaStreamSynchronize(g->stream));
     kresolve(g);
     if (out_iters) *out_iters = iters;
@@ -666,8 +746,6 @@ const char* fl_last_error(void) { return g_err.c_str(); }
 int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
                     const double* area, const uint32_t* default_outlets, uint32_t n_default,
                     const double* xs, const double* ys, fl_graph** out) {
-    (void)xs;
-    (void)ys;
     g_err.clear();
     if (!out || !row_ptr || (!col && n) || !area || (n_default && !default_outlets) || n == 0 ||
         n >= kNone) {
@@ -695,10 +773,19 @@ int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, co
     if (cudaGetDevice(&g->device) != cudaSuccess) g->device = 0;
     g->n = n;
     g->nnz = nnz;
-    g->h_row.assign(row_ptr, row_ptr + n + 1);
-    g->h_col.assign(col, col + nnz);
-    g->h_len.assign(len, len + nnz);
-    g->def_outlets.assign(default_outlets, default_outlets + n_default);
+    if (xs && ys) {
+        fl::hilbert_order(n, xs, ys, g->perm);
+    } else {
+        g->perm.resize(n);
+        for (uint32_t i = 0; i < n; ++i) g->perm[i] = i;
+    }
+    g->inv.resize(n);
+    for (uint32_t j = 0; j < n; ++j) g->inv[g->perm[j]] = j;
+    fl::relabel_csr(n, row_ptr, col, len, g->perm, g->inv, g->h_row, g->h_col, g->h_len);
+    g->def_outlets.resize(n_default);
+    for (uint32_t i = 0; i < n_default; ++i) g->def_outlets[i] = g->inv[default_outlets[i]];
+    std::vector<double> parea(n);
+    for (uint32_t j = 0; j < n; ++j) parea[j] = area[g->perm[j]];
     int rc = FL_OK;
     auto fail = [&](int r) { free_graph(g); return r; };
     cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
@@ -708,12 +795,15 @@ int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, co
         return fail(FL_ERR_CUDA);
     }
     if ((rc = dalloc(&g->d_row, n + 1)) || (rc = dalloc(&g->d_col, nnz)) ||
-        (rc = dalloc(&g->d_len, nnz)) || (rc = dalloc(&g->d_area, n)) || (rc = alloc_workspace(g)))
+        (rc = dalloc(&g->d_len, nnz)) || (rc = dalloc(&g->d_area, n)) ||
+        (rc = dalloc(&g->d_perm, n)) || (rc = dalloc(&g->d_inv, n)) || (rc = alloc_workspace(g)))
         return fail(rc);
-    if (cudaMemcpy(g->d_row, row_ptr, (n + 1) * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
-        (nnz && cudaMemcpy(g->d_col, col, nnz * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) ||
-        (nnz && cudaMemcpy(g->d_len, len, nnz * 8ull, cudaMemcpyHostToDevice) != cudaSuccess) ||
-        cudaMemcpy(g->d_area, area, n * 8ull, cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (cudaMemcpy(g->d_row, g->h_row.data(), (n + 1) * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (nnz && cudaMemcpy(g->d_col, g->h_col.data(), nnz * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        (nnz && cudaMemcpy(g->d_len, g->h_len.data(), nnz * 8ull, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        cudaMemcpy(g->d_area, parea.data(), n * 8ull, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->d_perm, g->perm.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->d_inv, g->inv.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) {
         g_err = "graph upload failed";
         return fail(FL_ERR_CUDA);
     }
@@ -741,17 +831,23 @@ int fl_generate_timed(fl_graph* g, uint32_t n_params, const double* base,
                          max_iteration, out_elev, out_iterations, loop_ms, total_ms);
 }
 
+// The probes take and return caller-order arrays and site ids.
 int fl_probe_receivers(fl_graph* g, const double* elev, const uint8_t* outlet_table,
                        uint32_t* next_out, int* has_lake) {
     if (!g) return FL_ERR_MODEL_NOT_SET;
     FL_CU(cudaSetDevice(g->device));
     uint32_t n = g->n;
-    FL_CU(cudaMemcpyAsync(g->d_elev, elev, n * 8ull, cudaMemcpyHostToDevice, g->stream));
-    FL_CU(cudaMemcpyAsync(g->d_outlet, outlet_table, n, cudaMemcpyHostToDevice, g->stream));
+    std::vector<uint8_t> table(n);
+    for (uint32_t j = 0; j < n; ++j) table[j] = outlet_table[g->perm[j]];
+    FL_TRY(upload_permuted(g, elev, g->d_elev));
+    FL_CU(cudaMemcpyAsync(g->d_outlet, table.data(), n, cudaMemcpyHostToDevice, g->stream));
+    FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
     int hl = 0;
     FL_TRY(run_receivers(g, &hl));
-    FL_CU(cudaMemcpyAsync(next_out, g->d_next, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
+    std::vector<uint32_t> nx(n);
+    FL_CU(cudaMemcpyAsync(nx.data(), g->d_next, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
     FL_CU(cudaStreamSynchronize(g->stream));
+    for (uint32_t i = 0; i < n; ++i) next_out[i] = g->perm[nx[g->inv[i]]];
     if (has_lake) *has_lake = hl;
     return FL_OK;
 }
@@ -761,19 +857,23 @@ int fl_probe_lakes(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     if (!g) return FL_ERR_MODEL_NOT_SET;
     FL_CU(cudaSetDevice(g->device));
     uint32_t n = g->n;
-    std::vector<uint32_t> o(outlets, outlets + n_outlets);
-    FL_TRY(set_outlets(g, o, true));
+    FL_TRY(set_outlets(g, to_device_ids(g, outlets, n_outlets), true));
     FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
-    FL_CU(cudaMemcpyAsync(g->d_next, next_in, n * 4ull, cudaMemcpyHostToDevice, g->stream));
+    std::vector<uint32_t> nx(n);
+    for (uint32_t j = 0; j < n; ++j) nx[j] = g->inv[next_in[g->perm[j]]];
+    FL_CU(cudaMemcpyAsync(g->d_next, nx.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
     std::vector<double> ones(n, 1.0);
     FL_CU(cudaMemcpyAsync(g->d_rlen, ones.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
     FL_TRY(run_labels(g));
-    if (label_out) {
-        FL_CU(cudaMemcpyAsync(label_out, g->d_lab, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
-    }
+    std::vector<uint32_t> lab(n);
+    FL_CU(cudaMemcpyAsync(lab.data(), g->d_lab, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
     FL_TRY(run_lakes(g));
-    FL_CU(cudaMemcpyAsync(next_out, g->d_next, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaMemcpyAsync(nx.data(), g->d_next, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
     FL_CU(cudaStreamSynchronize(g->stream));
+    for (uint32_t i = 0; i < n; ++i) {
+        next_out[i] = g->perm[nx[g->inv[i]]];
+        if (label_out) label_out[i] = g->perm[lab[g->inv[i]]];
+    }
     return FL_OK;
 }
 
@@ -784,40 +884,50 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     if (!g) return FL_ERR_MODEL_NOT_SET;
     FL_CU(cudaSetDevice(g->device));
     uint32_t n = g->n;
-    std::vector<uint32_t> o(outlets, outlets + n_outlets);
     FL_TRY(upload_params(g, nullptr, erodibility, uplift, max_slope));
-    FL_TRY(set_outlets(g, o, false));
-    FL_CU(cudaMemcpyAsync(g->d_next, next, n * 4ull, cudaMemcpyHostToDevice, g->stream));
-    FL_CU(cudaMemcpyAsync(g->d_elev, elev, n * 8ull, cudaMemcpyHostToDevice, g->stream));
-    // receiver lengths as has_edge reports them
+    FL_TRY(set_outlets(g, to_device_ids(g, outlets, n_outlets), false));
+    std::vector<uint32_t> nx(n);
+    for (uint32_t j = 0; j < n; ++j) nx[j] = g->inv[next[g->perm[j]]];
+    FL_CU(cudaMemcpyAsync(g->d_next, nx.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
+    FL_TRY(upload_permuted(g, elev, g->d_elev));
+    // receiver lengths as has_edge reports them (device order)
     std::vector<double> rl(n);
-    for (uint32_t i = 0; i < n; ++i) {
-        rl[i] = 1.0;
-        if (next[i] != i)
-            for (uint32_t s = g->h_row[i]; s < g->h_row[i + 1]; ++s)
-                if (g->h_col[s] == next[i]) { rl[i] = g->h_len[s]; break; }
+    for (uint32_t j = 0; j < n; ++j) {
+        rl[j] = 1.0;
+        if (nx[j] != j)
+            for (uint32_t s = g->h_row[j]; s < g->h_row[j + 1]; ++s)
+                if (g->h_col[s] == nx[j]) { rl[j] = g->h_len[s]; break; }
     }
     FL_CU(cudaMemcpyAsync(g->d_rlen, rl.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
     k_fill_f64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_A, g->d_area);
-    k_fill_f64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_t, nullptr);
     FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
     int ch = 0;
     FL_TRY(run_basin_pass(g, &ch));
-    FL_CU(cudaMemcpyAsync(elev, g->d_elev, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
-    if (drainage_out) FL_CU(cudaMemcpyAsync(drainage_out, g->d_A, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
-    if (response_out) FL_CU(cudaMemcpyAsync(response_out, g->d_t, n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_TRY(download_permuted(g, g->d_elev, elev));
     FL_CU(cudaStreamSynchronize(g->stream));
+    if (drainage_out) {
+        FL_TRY(download_permuted(g, g->d_A, drainage_out));
+        FL_CU(cudaStreamSynchronize(g->stream));
+    }
+    if (response_out) {
+        FL_TRY(download_permuted(g, g->d_t, response_out));
+        FL_CU(cudaStreamSynchronize(g->stream));
+    }
     if (changed) *changed = ch;
     return FL_OK;
 }
 
 int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets, uint32_t* rank) {
     if (!g) return FL_ERR_MODEL_NOT_SET;
-    if (!fl::lake_heap_rank(g->n, g->h_row.data(), g->h_col.data(), g->h_len.data(), outlets,
-                            n_outlets, rank)) {
+    std::vector<uint32_t> o = to_device_ids(g, outlets, n_outlets);
+    std::vector<uint32_t> r(g->n);
+    if (!fl::lake_heap_rank(g->n, g->h_row.data(), g->h_col.data(), g->h_len.data(), o.data(),
+                            n_outlets, r.data())) {
         g_err = "NaN edge length in the lake traversal";
         return FL_ERR_INVALID_ARGUMENT;
     }
+    for (uint32_t i = 0; i < g->n; ++i) rank[i] = r[g->inv[i]];
     return FL_OK;
 }
 
@@ -842,6 +952,14 @@ void fl_graph_reset_stats(fl_graph* g) {
 }
 
 uint32_t fl_num_kernel_classes(void) { return kcCount; }
+
+int fl_graph_basin_stats(const fl_graph* g, uint64_t* out, uint32_t cap) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    const uint32_t idx[] = {kMetaRStop, kMetaLeaves, kMetaNs, kMetaChains, kMetaMaxChain,
+                            kMetaSlow, kMetaSpinUp, kMetaSpinDown};
+    for (uint32_t i = 0; i < cap && i < sizeof idx / sizeof idx[0]; ++i) out[i] = g->last_meta[idx[i]];
+    return FL_OK;
+}
 
 int fl_graph_kernel_stats(const fl_graph* g, uint32_t cls, const char** name, uint64_t* launches,
                           double* device_ms, double* bytes) {

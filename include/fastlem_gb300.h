@@ -111,6 +111,11 @@ uint32_t fl_num_kernel_classes(void);
 int fl_graph_kernel_stats(const fl_graph* g, uint32_t cls, const char** name, uint64_t* launches,
                           double* device_ms, double* bytes);
 
+/* Shape of the last basin pass (up to `cap` values): Kahn rounds run, leaves,
+ * skeleton sites, skeleton chains, longest chain, skeleton sites needing the full
+ * pull while walking, bottom-up and top-down hand-off wait iterations. */
+int fl_graph_basin_stats(const fl_graph* g, uint64_t* out, uint32_t cap);
+
 /* ---- parity probes: one solver stage on host arrays (tests only) ---------------- */
 
 /* Steepest-descent receivers (lem/stream_tree.rs:109-137); outlet_table[i] != 0 keeps
