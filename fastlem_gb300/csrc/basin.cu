@@ -40,20 +40,52 @@
 namespace fl {
 namespace {
 
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // per-slot flags of the skeleton layout
 constexpr uint8_t kLeafSlot = 1;   // chain leaf: pre holds the complete area
 constexpr uint8_t kSlow = 4;       // confluence or > kMaxPost additions: full pull at walk time
 constexpr int kPostShift = 3;      // bits 3-4: additions after the chain predecessor (0..3)
 constexpr int kMaxPost = 3;
 
+// Rows up to this many slots are gathered with all loads in flight at once; longer
+// rows (rare: hull sites) take the plain loop.
+constexpr int kRowFast = 12;
+
+// The reference's drainage area of v given final donor areas: a_v + donors in
+// reverse adjacency order (generator.rs:154-159).  Column ids, then receivers,
+// then donor areas are each loaded together, so a row costs three memory latencies
+// rather than three per slot.
 __device__ __forceinline__ double pull_area(uint32_t v, const uint32_t* __restrict__ row,
                                             const uint32_t* __restrict__ col,
                                             const uint32_t* __restrict__ next,
                                             const double* __restrict__ area, const double* A) {
+    const uint32_t s0 = row[v], s1 = row[v + 1];
     double a = area[v];
-    for (uint32_t s = row[v + 1]; s-- > row[v];) {
-        uint32_t d = col[s];
-        if (d != v && next[d] == v) a = __dadd_rn(a, __ldcg(&A[d]));
+    const uint32_t deg = s1 - s0;
+    if (deg <= (uint32_t)kRowFast) {
+        uint32_t d[kRowFast];
+        bool don[kRowFast];
+        double val[kRowFast];
+#pragma unroll
+        for (int k = 0; k < kRowFast; ++k)
+            if ((uint32_t)k < deg) d[k] = col[s0 + k];
+#pragma unroll
+        for (int k = 0; k < kRowFast; ++k)
+            don[k] = (uint32_t)k < deg && d[k] != v && next[d[k]] == v;
+#pragma unroll
+        for (int k = 0; k < kRowFast; ++k)
+            if (don[k]) val[k] = __ldcg(&A[d[k]]);
+#pragma unroll
+        for (int k = kRowFast - 1; k >= 0; --k)
+            if (don[k]) a = __dadd_rn(a, val[k]);
+        return a;
+    }
+    for (uint32_t s = s1; s-- > s0;) {
+        uint32_t dd = col[s];
+        if (dd != v && next[dd] == v) a = __dadd_rn(a, __ldcg(&A[dd]));
     }
     return a;
 }
@@ -70,7 +102,8 @@ __global__ void k_collect_leaves(uint32_t n, const uint32_t* __restrict__ pendin
                                  uint32_t* __restrict__ order, uint32_t* __restrict__ counter) {
     uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
-    if (pending[v] == 0) order[atomicAdd(counter, 1u)] = v;
+    uint32_t pos = warp_append(counter, pending[v] == 0);
+    if (pos != kNone) order[pos] = v;
 }
 
 // Kahn rounds.  order[0, nleaves) holds the leaves; rounds append the next frontier
@@ -100,8 +133,10 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
             A[v] = (r == 0) ? area[v] : pull_area(v, row, col, next, area, A);
             hgt[v] = r;
             uint32_t p = next[v];
-            if (p != v && atomicSub(&pending[p], 1u) == 1u) {
-                uint32_t pos = end + atomicAdd(cnt, 1u);
+            bool ready = p != v && atomicSub(&pending[p], 1u) == 1u;
+            uint32_t pos = warp_append(cnt, ready);
+            if (pos != kNone) {
+                pos += end;
                 if (pos < n) order[pos] = p;
                 else set_error(flags, kErrForest);
             }
@@ -134,8 +169,8 @@ __global__ void k_s_collect(uint32_t n, const uint32_t* __restrict__ hgt,
                             uint32_t* meta) {
     uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
-    if (hgt[v] == kNone) {
-        uint32_t k = atomicAdd(&meta[kMetaNs], 1u);
+    uint32_t k = warp_append(&meta[kMetaNs], hgt[v] == kNone);
+    if (k != kNone) {
         sid[v] = k;
         slist[k] = v;
     }
@@ -201,7 +236,7 @@ __global__ void k_s_rank(uint32_t* ptr0, uint32_t* dist0, uint32_t* ptr1, uint32
             P[cur ^ 1][k] = pp;
             changed |= (pp != p);
         }
-        if (changed) atomicOr(jf, 1u);
+        if (__syncthreads_or(changed) && threadIdx.x == 0) atomicOr(jf, 1u);
         if (!grid_barrier(flags)) return;
         cur ^= 1;
         if (ld_acquire_u(jf) == 0) {
@@ -352,7 +387,7 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
         post1[q] = ps[1];
         post2[q] = ps[2];
         sflag[q] = f | (uint8_t)(np << kPostShift);
-        if (f & kSlow) atomicAdd(&meta[kMetaSlow], 1u);
+        warp_append(&meta[kMetaSlow], (f & kSlow) != 0);
     }
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         uint32_t b = cbot[c];
@@ -442,7 +477,16 @@ __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* 
     while (q >= (int32_t)off) {
         double np[kBatch], nq[kBatch], nr[kBatch], ns[kBatch];
         uint8_t nf[kBatch];
-        load(q - kBatch, np, nq, nr, ns, nf);    // next batch in flight
+        // lines of the batch three ahead go to L1 now; the batch after next is in flight
+        int32_t pf = q - 4 * kBatch + 1;
+        if (pf >= (int32_t)off) {
+            prefetch_l1(pre + pf);
+            prefetch_l1(post + pf);
+            prefetch_l1(post1 + pf);
+            prefetch_l1(post2 + pf);
+            prefetch_l1(sflag + pf);
+        }
+        load(q - kBatch, np, nq, nr, ns, nf);
 #pragma unroll
         for (int i = 0; i < kBatch; ++i) {
             int32_t qq = q - i;
@@ -529,7 +573,7 @@ struct TopDown {
 // For a root, (tp, ep, o) are ignored.  Returns t_v; writes t, bas, elev.
 __device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t p, double tp,
                                          uint32_t o, double to, double eo, double ep,
-                                         double* e_out) {
+                                         double* e_out, bool* changed) {
     double tv;
     double old_e = __ldcg(&td.elev[v]);
     if (p == v) {                         // root: t = 0 + (0 + w), o = v
@@ -553,7 +597,7 @@ __device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t
             double slope = __ddiv_rn(__dsub_rn(ne, ep), dist);
             if (slope > tn) ne = __dadd_rn(ep, __dmul_rn(tn, dist));
         }
-        if (ne != old_e) td.flags[kChanged] = 1;
+        if (ne != old_e) *changed = true;
         td.elev[v] = ne;
     }
     *e_out = ne;
@@ -584,9 +628,10 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
     double tp, ep, to = 0.0, eo = 0.0;
     uint32_t o = kNone;
     uint32_t q = off;
+    bool changed = false;
     if (p == v) {                         // the chain starts at a root
         double e;
-        tp = settle(td, v, p, 0.0, kNone, 0.0, 0.0, 0.0, &e);
+        tp = settle(td, v, p, 0.0, kNone, 0.0, 0.0, 0.0, &e, &changed);
         ep = e;
         o = td.outlet[v] ? v : kNone;
         to = tp;
@@ -633,6 +678,11 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
         while (q < end) {
             double nw[kBatch];
             uint8_t nn[kBatch];
+            if (q + 4 * kBatch < end) {
+                prefetch_l1(wl + q + 4 * kBatch);
+                prefetch_l1(wl + q + 5 * kBatch - 1);
+                prefetch_l1(needl + q + 4 * kBatch);
+            }
 #pragma unroll
             for (int i = 0; i < kBatch; ++i) {
                 if (q + kBatch + i < end) {
@@ -643,7 +693,8 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
 #pragma unroll
             for (int i = 0; i < kBatch; ++i) {
                 if (q + i >= end) break;
-                tp = plus_zero(__dadd_rn(tp, bw[i]));
+                // below a root t is never -0.0, so 0 + (t_p + w) is just t_p + w
+                tp = __dadd_rn(tp, bw[i]);
                 tl[q + i] = tp;
                 if (bn[i]) {                   // another chain hangs here: publish t, elev, bas
                     uint32_t u = layout[q + i];
@@ -651,7 +702,7 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
                     if (o != kNone) {
                         double dt = __dsub_rn(tp, to);
                         e = __dadd_rn(eo, __dmul_rn(td.uu[u], dt > 0.0 ? dt : 0.0));
-                        if (e != __ldcg(&td.elev[u])) td.flags[kChanged] = 1;
+                        if (e != __ldcg(&td.elev[u])) changed = true;
                     }
                     td.t[u] = tp;
                     td.elev[u] = e;
@@ -671,7 +722,7 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
         for (; q < end; ++q) {
             v = layout[q];
             double e;
-            tp = settle(td, v, p, tp, o, to, eo, ep, &e);
+            tp = settle(td, v, p, tp, o, to, eo, ep, &e, &changed);
             tl[q] = tp;
             el[q] = e;
             ep = e;
@@ -682,6 +733,7 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
             }
         }
     }
+    if (changed) td.flags[kChanged] = 1;
 }
 
 // Skeleton response times and elevations back to site order.
@@ -692,6 +744,7 @@ __global__ void k_s_finish(TopDown td, const uint32_t* __restrict__ layout,
                            bool slope, const uint32_t* meta) {
     if (td.flags[kError]) return;
     uint32_t ns = meta[kMetaNs];
+    bool changed = false;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x) {
         uint32_t v = layout[q];
         if (td.next[v] == v) continue;     // roots were settled by the walker
@@ -709,9 +762,10 @@ __global__ void k_s_finish(TopDown td, const uint32_t* __restrict__ layout,
             double dt = __dsub_rn(tv, cto[c]);
             ne = __dadd_rn(ceo[c], __dmul_rn(td.uu[v], dt > 0.0 ? dt : 0.0));
         }
-        if (ne != old_e) td.flags[kChanged] = 1;
+        if (ne != old_e) changed = true;
         td.elev[v] = ne;
     }
+    block_flag(td.flags, kChanged, changed);
 }
 
 // Top-down over the Kahn rounds, highest round first.
@@ -721,6 +775,7 @@ __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
     const uint32_t stride = gridDim.x * blockDim.x;
     if (ld_acquire(&td.flags[kError])) return;
     uint32_t rs = meta[kMetaRStop];
+    bool changed = false;
     for (uint32_t r = rs; r-- > 0;) {
         uint32_t b = roff[r], e = roff[r + 1];
         for (uint32_t i = b + gtid; i < e; i += stride) {
@@ -738,10 +793,11 @@ __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
                 }
             }
             double en;
-            settle(td, v, p, tp, o, to, eo, ep, &en);
+            settle(td, v, p, tp, o, to, eo, ep, &en, &changed);
         }
         if (!grid_barrier(td.flags)) return;
     }
+    block_flag(td.flags, kChanged, changed);
 }
 
 template <class K, class... Args>
@@ -750,24 +806,28 @@ cudaError_t coop_launch(K kernel, unsigned grid, unsigned block, cudaStream_t st
     return cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(block), argv, 0, st);
 }
 
-// Blocks of kThreads at which `kernel` is co-resident on the current device.
-unsigned coop_grid(const void* kernel, unsigned cap_per_sm) {
+// Blocks of `block` threads at which `kernel` is co-resident on the current device.
+unsigned coop_grid(const void* kernel, unsigned block, unsigned cap_per_sm) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, (int)block, 0);
     if (per < 1) per = 1;
     return (unsigned)(sms * std::min<unsigned>((unsigned)per, cap_per_sm));
 }
+
+// Round kernels synchronise the grid every round; big blocks keep the number of
+// barrier arrivals (one per block) small.
+constexpr unsigned kRoundBlock = 1024;
 
 }  // namespace
 
 cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz) {
     const uint32_t n = a.n;
     const unsigned nb = (n + kThreads - 1) / kThreads;
-    const unsigned g_kahn = coop_grid((const void*)k_kahn, 8);
-    const unsigned g_rank = coop_grid((const void*)k_s_rank, 8);
-    const unsigned g_low = coop_grid((const void*)k_low_top_down, 8);
+    const unsigned g_kahn = coop_grid((const void*)k_kahn, kRoundBlock, 2);
+    const unsigned g_rank = coop_grid((const void*)k_s_rank, kRoundBlock, 2);
+    const unsigned g_low = coop_grid((const void*)k_low_top_down, kRoundBlock, 2);
     const unsigned g_chain = (a.kahn_min_width + kThreads - 1) / kThreads;
     const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
@@ -785,7 +845,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     // Kahn rounds: order 4 + next 4 + row 8 + area 8 + A 8 + hgt 4 + pending 4 per site,
     // col 4 + next 4 per slot, donor areas 8 per site
     hk.begin(hk.ctx);
-    e = coop_launch(k_kahn, g_kahn, kThreads, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
+    e = coop_launch(k_kahn, g_kahn, kRoundBlock, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
                     a.hgt, a.order, a.roff, a.max_rounds, a.kahn_min_width, a.meta, a.flags);
     hk.end(hk.ctx, kcKahn, 48.0 * n + 8.0 * nnz);
     if (e != cudaSuccess) return e;
@@ -799,7 +859,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     hk.end(hk.ctx, kcBasinBuild, 4.0 * n);
 
     hk.begin(hk.ctx);
-    e = coop_launch(k_s_rank, g_rank, kThreads, st, a.sptr0, a.sdist0, a.sptr1, a.sdist1, a.meta,
+    e = coop_launch(k_s_rank, g_rank, kRoundBlock, st, a.sptr0, a.sdist0, a.sptr1, a.sdist1, a.meta,
                     a.flags);
     hk.end(hk.ctx, kcSkelRank, 0.0);
     if (e != cudaSuccess) return e;
@@ -861,7 +921,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     // top-down rounds: order 4, next 4, w 8, u 8, tan 8, rlen 8, elev 8+8, t 8, bas 4,
     // parent t/elev/bas 20, outlet t/elev 16 per site
     hk.begin(hk.ctx);
-    e = coop_launch(k_low_top_down, g_low, kThreads, st, td, (const uint32_t*)a.order,
+    e = coop_launch(k_low_top_down, g_low, kRoundBlock, st, td, (const uint32_t*)a.order,
                     (const uint32_t*)a.roff, (const uint32_t*)a.meta);
     hk.end(hk.ctx, kcLowDown, 112.0 * n);
     return e;

@@ -77,9 +77,10 @@ __device__ __forceinline__ bool grid_barrier(int* flags) {
                 __nanosleep(64);
             }
         }
+        if (ld_acquire(&flags[kError]) != 0) ok = 0;
     }
     __syncthreads();
-    return ok && ld_acquire(&flags[kError]) == 0;
+    return ok != 0;   // the same verdict for every thread of the block
 }
 
 // Waits (bounded) until *flag becomes nonzero.  Returns false on timeout / error.
@@ -94,6 +95,26 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int* flags) {
         __nanosleep(32);
     }
     return true;
+}
+
+// Appends for every lane with pred set: one atomicAdd per warp instead of one per
+// lane (same-address atomics serialise in L2).  Returns the lane's slot, or kNone.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    const unsigned mask = __activemask();
+    const unsigned ballot = __ballot_sync(mask, pred);
+    if (!pred) return kNone;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(ballot));
+    base = __shfl_sync(ballot, base, leader);
+    return base + (uint32_t)__popc(ballot & ((1u << lane) - 1u));
+}
+
+// Raises flags[slot] once per block if any thread's pred is set.  Every thread of
+// the block must call it (it contains __syncthreads).
+__device__ __forceinline__ void block_flag(int* flags, int slot, bool pred) {
+    if (__syncthreads_or(pred) && threadIdx.x == 0) flags[slot] = 1;
 }
 
 // `0.0 + x` exactly as IEEE evaluates it: x itself, except that -0.0 becomes +0.0.

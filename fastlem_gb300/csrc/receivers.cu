@@ -23,6 +23,7 @@ namespace fl {
 namespace {
 
 constexpr uint64_t kMant = (1ull << 52) - 1;
+constexpr int kRowFast = 12;   // rows up to this length gather their elevations at once
 
 // Float estimate of (a - b) for non-negative finite doubles with bits A > B.
 // Returns false when the result falls outside the normal f32 range.
@@ -63,13 +64,13 @@ __device__ __forceinline__ bool to_float_estimate(uint64_t L, float& out) {
     return true;
 }
 
-__global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
-                            const uint32_t* __restrict__ col, const double* __restrict__ len,
-                            const double* __restrict__ elev, const uint8_t* __restrict__ outlet,
-                            uint32_t* __restrict__ next, double* __restrict__ rlen,
-                            int* __restrict__ flags) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void scan_site(uint32_t i, const uint32_t* __restrict__ row,
+                                          const uint32_t* __restrict__ col,
+                                          const double* __restrict__ len,
+                                          const double* __restrict__ elev,
+                                          const uint8_t* __restrict__ outlet,
+                                          uint32_t* __restrict__ next, double* __restrict__ rlen,
+                                          bool* lake, bool* went_exact) {
     if (outlet[i]) {
         next[i] = i;
         rlen[i] = 1.0;
@@ -83,19 +84,20 @@ __global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
     uint32_t best_slot = kNone;
     bool any_lower = false;
     if (!exact) {
-        for (uint32_t s = s0; s < s1; ++s) {
-            const uint64_t EJ = (uint64_t)__double_as_longlong(elev[col[s]]);
-            if ((EJ >> 63) || (EJ >> 52) == 0x7ff) { exact = true; break; }
-            if (EI <= EJ) continue;                         // not lower (bits are monotone)
+        // one candidate: exact comparison of the bit patterns, then the f32 estimate
+        auto consider = [&](uint32_t s, uint64_t EJ) {
+            if (exact) return;
+            if ((EJ >> 63) || (EJ >> 52) == 0x7ff) { exact = true; return; }
+            if (EI <= EJ) return;                          // not lower (bits are monotone)
             any_lower = true;
             float d, l;
             if (!diff_estimate(EI, EJ, d) ||
                 !to_float_estimate((uint64_t)__double_as_longlong(len[s]), l)) {
                 exact = true;
-                break;
+                return;
             }
             float a = __fdividef(d, l);
-            if (!(a > 1e-30f) || !(a < 1e30f)) { exact = true; break; }
+            if (!(a > 1e-30f) || !(a < 1e30f)) { exact = true; return; }
             if (a > best) {
                 second = best;
                 best = a;
@@ -103,12 +105,30 @@ __global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
             } else if (a > second) {
                 second = a;
             }
+        };
+        const uint32_t deg = s1 - s0;
+        if (deg <= (uint32_t)kRowFast) {
+            // short rows: all neighbour elevations in flight at once
+            uint32_t jj[kRowFast];
+            uint64_t ej[kRowFast];
+#pragma unroll
+            for (int k = 0; k < kRowFast; ++k)
+                if ((uint32_t)k < deg) jj[k] = col[s0 + k];
+#pragma unroll
+            for (int k = 0; k < kRowFast; ++k)
+                if ((uint32_t)k < deg) ej[k] = (uint64_t)__double_as_longlong(elev[jj[k]]);
+#pragma unroll
+            for (int k = 0; k < kRowFast; ++k)
+                if ((uint32_t)k < deg) consider(s0 + k, ej[k]);
+        } else {
+            for (uint32_t s = s0; s < s1; ++s)
+                consider(s, (uint64_t)__double_as_longlong(elev[col[s]]));
         }
         if (!exact && any_lower && second > best * (1.0f - 7.62939453125e-06f)) exact = true;
     }
     uint32_t nb = i;
     if (exact) {
-        atomicAdd(&flags[kExact], 1);
+        *went_exact = true;
         double steepest = 0.0;
         best_slot = kNone;
         for (uint32_t s = s0; s < s1; ++s) {
@@ -126,7 +146,7 @@ __global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
     if (best_slot == kNone) {
         next[i] = i;
         rlen[i] = 1.0;
-        flags[kHasLake] = 1;
+        *lake = true;
         return;
     }
     nb = col[best_slot];
@@ -134,6 +154,19 @@ __global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
     uint32_t s = s0;
     while (col[s] != nb) ++s;   // first entry of the receiver, as has_edge reports it
     rlen[i] = len[s];
+}
+
+
+__global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
+                            const uint32_t* __restrict__ col, const double* __restrict__ len,
+                            const double* __restrict__ elev, const uint8_t* __restrict__ outlet,
+                            uint32_t* __restrict__ next, double* __restrict__ rlen,
+                            int* __restrict__ flags) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool lake = false, went_exact = false;
+    if (i < n) scan_site(i, row, col, len, elev, outlet, next, rlen, &lake, &went_exact);
+    block_flag(flags, kHasLake, lake);
+    if (__syncthreads_or(went_exact) && threadIdx.x == 0) atomicAdd(&flags[kExact], 1);
 }
 
 }  // namespace
