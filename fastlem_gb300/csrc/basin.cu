@@ -396,46 +396,69 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
     }
 }
 
-// Full pull of v at walk time: heavy donor's value is x, other skeleton donors are
-// chain bottoms published through bu_done.
-__device__ double slow_pull(uint32_t v, uint32_t heavy, double x, const uint32_t* __restrict__ row,
-                            const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
-                            const uint32_t* __restrict__ hgt, const double* __restrict__ area,
-                            const double* A, const int* bu_done, int stamp, int* flags, bool* ok,
-                            uint32_t* spin_total) {
-    double a = area[v];
-    for (uint32_t s = row[v + 1]; s-- > row[v];) {
-        uint32_t d = col[s];
-        if (d == v || next[d] != v) continue;
-        double val;
-        if (d == heavy) {
-            val = x;
-        } else {
-            if (hgt[d] == kNone) {
-                uint32_t spins = 0;
-                while (ld_acquire(&bu_done[d]) != stamp) {
-                    if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&flags[kError]))) {
-                        set_error(flags, kErrWait);
-                        *ok = false;
-                        return 0.0;
+constexpr int kBatch = 8;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Full pull of v during the walk, by the whole warp: lane l takes slot s1-1-l (reverse
+// row order), the values are folded in lane order.  The chain predecessor's value is
+// x; another skeleton donor is a chain bottom, waited for through bu_done.
+__device__ double warp_slow_pull(uint32_t v, uint32_t heavy, double x,
+                                 const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
+                                 const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
+                                 const double* __restrict__ area, const double* A,
+                                 const int* bu_done, int stamp, int* flags, bool* ok,
+                                 uint32_t* spin_total) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t s0 = row[v], s1 = row[v + 1];
+    double acc = area[v];
+    bool fail = false;
+    for (int64_t hi = s1; hi > (int64_t)s0; hi -= 32) {
+        const int64_t s = hi - 1 - lane;
+        bool don = false;
+        double val = 0.0;
+        if (s >= (int64_t)s0) {
+            uint32_t d = col[s];
+            if (d != v && next[d] == v) {
+                don = true;
+                if (d == heavy) {
+                    val = x;
+                } else {
+                    if (hgt[d] == kNone) {
+                        uint32_t spins = 0;
+                        while (ld_acquire(&bu_done[d]) != stamp) {
+                            if (++spins > kSpinLimit ||
+                                ((spins & 255) == 0 && ld_acquire(&flags[kError]))) {
+                                set_error(flags, kErrWait);
+                                fail = true;
+                                break;
+                            }
+                            __nanosleep(32);
+                        }
+                        *spin_total += spins;
                     }
-                    __nanosleep(32);
+                    val = __ldcg(&A[d]);
                 }
-                *spin_total += spins;
             }
-            val = __ldcg(&A[d]);
         }
-        a = __dadd_rn(a, val);
+        unsigned dm = __ballot_sync(kFull, don);
+        if (__any_sync(kFull, fail)) {
+            *ok = false;
+            return 0.0;
+        }
+        while (dm) {
+            int j = __ffs(dm) - 1;
+            acc = __dadd_rn(acc, __shfl_sync(kFull, val, j));
+            dm &= dm - 1;
+        }
     }
-    return a;
+    return acc;
 }
 
-constexpr int kBatch = 8;
-
-// One thread per chain, leaf to bottom.  Operands are read in layout order in
-// batches of kBatch, the next batch's loads issued before the current batch's
-// dependent additions.  Results go to Al (layout order); the chain bottom's area
-// is also stored in A and published through bu_done.
+// One warp per chain, leaf to bottom.  Each round the lanes load 32 slots (coalesced)
+// into shared memory and issue the next 32 slots' loads; then every lane replays the
+// 32 dependent additions (identical, so branches are warp-uniform) and lane i keeps
+// the result of slot i.  Results go to Al (layout order); the chain bottom's area is
+// also stored in A and published through bu_done.
 __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
                               const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
                               const double* __restrict__ area, double* A,
@@ -445,83 +468,78 @@ __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* 
                               const double* __restrict__ post1, const double* __restrict__ post2,
                               const uint8_t* __restrict__ sflag, double* __restrict__ Al,
                               int* bu_done, int stamp, uint32_t* meta, int* flags) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= meta[kMetaChains] || flags[kError]) return;
+    __shared__ double sv[kWalkWarps][2][4][32];
+    __shared__ uint8_t sf[kWalkWarps][2][32];
+    const int lane = threadIdx.x & 31;
+    const int wb = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * kWalkWarps + wb;
+    // warp-uniform exits only: the warp shuffles with the full mask below
+    if (c >= meta[kMetaChains] || __any_sync(kFull, ld_acquire(&flags[kError]) != 0)) return;
     const uint32_t off = coff[c];
     const uint32_t len = clen[c];
     if (off + len > meta[kMetaNs] || len == 0) {
-        set_error(flags, kErrForest);
+        if (lane == 0) set_error(flags, kErrForest);
         return;
     }
+    const int64_t lo = off;
+    int64_t top = (int64_t)off + len - 1;
+    double rp = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0;
+    uint8_t rf = 0;
+    auto load = [&](int64_t t) {
+        int64_t q = t - lane;
+        if (q >= lo) {
+            rp = pre[q];
+            r0 = post[q];
+            r1 = post1[q];
+            r2 = post2[q];
+            rf = sflag[q];
+        }
+    };
+    load(top);
     double x = 0.0;
     bool ok = true;
     uint32_t spins = 0;
-    // positions are processed from hi = off + len - 1 down to off
-    int32_t q = (int32_t)(off + len) - 1;
-    double bp[kBatch], bq[kBatch], br[kBatch], bs[kBatch];
-    uint8_t bf[kBatch];
-    auto load = [&](int32_t top, double* P, double* Q, double* R, double* S, uint8_t* F) {
-#pragma unroll
-        for (int i = 0; i < kBatch; ++i) {
-            int32_t qq = top - i;
-            if (qq >= (int32_t)off) {
-                P[i] = pre[qq];
-                Q[i] = post[qq];
-                R[i] = post1[qq];
-                S[i] = post2[qq];
-                F[i] = sflag[qq];
-            }
-        }
-    };
-    load(q, bp, bq, br, bs, bf);
-    while (q >= (int32_t)off) {
-        double np[kBatch], nq[kBatch], nr[kBatch], ns[kBatch];
-        uint8_t nf[kBatch];
-        // lines of the batch three ahead go to L1 now; the batch after next is in flight
-        int32_t pf = q - 4 * kBatch + 1;
-        if (pf >= (int32_t)off) {
-            prefetch_l1(pre + pf);
-            prefetch_l1(post + pf);
-            prefetch_l1(post1 + pf);
-            prefetch_l1(post2 + pf);
-            prefetch_l1(sflag + pf);
-        }
-        load(q - kBatch, np, nq, nr, ns, nf);
-#pragma unroll
-        for (int i = 0; i < kBatch; ++i) {
-            int32_t qq = q - i;
-            if (qq < (int32_t)off) break;
-            uint8_t f = bf[i];
+    int cur = 0;
+    for (; top >= lo; top -= 32) {
+        sv[wb][cur][0][lane] = rp;
+        sv[wb][cur][1][lane] = r0;
+        sv[wb][cur][2][lane] = r1;
+        sv[wb][cur][3][lane] = r2;
+        sf[wb][cur][lane] = rf;
+        __syncwarp();
+        load(top - 32);                               // next round in flight
+        const int64_t left = top - lo + 1;
+        const int cnt = left < 32 ? (int)left : 32;
+        double mine = 0.0;
+        for (int i = 0; i < cnt; ++i) {
+            const uint8_t f = sf[wb][cur][i];
             if (f & kLeafSlot) {
-                x = bp[i];
+                x = sv[wb][cur][0][i];
             } else if (!(f & kSlow)) {
-                int npost = (f >> kPostShift) & 3;
-                x = __dadd_rn(bp[i], x);
-                if (npost > 0) x = __dadd_rn(x, bq[i]);
-                if (npost > 1) x = __dadd_rn(x, br[i]);
-                if (npost > 2) x = __dadd_rn(x, bs[i]);
+                const int np = (f >> kPostShift) & 3;
+                x = __dadd_rn(sv[wb][cur][0][i], x);
+                if (np > 0) x = __dadd_rn(x, sv[wb][cur][1][i]);
+                if (np > 1) x = __dadd_rn(x, sv[wb][cur][2][i]);
+                if (np > 2) x = __dadd_rn(x, sv[wb][cur][3][i]);
             } else {
-                x = slow_pull(layout[qq], layout[qq + 1], x, row, col, next, hgt, area, A, bu_done,
-                              stamp, flags, &ok, &spins);
+                x = warp_slow_pull(layout[top - i], layout[top - i + 1], x, row, col, next, hgt,
+                                   area, A, bu_done, stamp, flags, &ok, &spins);
                 if (!ok) return;
             }
-            Al[qq] = x;
+            if (lane == i) mine = x;
         }
-        q -= kBatch;
-#pragma unroll
-        for (int i = 0; i < kBatch; ++i) {
-            bp[i] = np[i];
-            bq[i] = nq[i];
-            br[i] = nr[i];
-            bs[i] = ns[i];
-            bf[i] = nf[i];
-        }
+        if (lane < cnt) Al[top - lane] = mine;
+        cur ^= 1;
+        __syncwarp();
     }
-    uint32_t bottom = layout[off];
-    A[bottom] = x;
-    __threadfence();
-    st_release(&bu_done[bottom], stamp);
-    if (spins) atomicAdd(&meta[kMetaSpinUp], spins);
+    if (lane == 0) {
+        uint32_t bottom = layout[off];
+        A[bottom] = x;
+        __threadfence();
+        st_release(&bu_done[bottom], stamp);
+    }
+    spins = __reduce_add_sync(kFull, spins);
+    if (lane == 0 && spins) atomicAdd(&meta[kMetaSpinUp], spins);
 }
 
 // Skeleton areas back to site order.
@@ -604,11 +622,12 @@ __device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t
     return tv;
 }
 
-// One thread per chain, bottom to leaf: t_v = 0 + (t_parent + w_v).  Without slope
-// limits only t is carried (tl, layout order; elevations follow in k_s_finish); with
-// them the elevation and its clamp against the receiver are carried too.  The chain's
-// basin outlet and its t / elevation are stored per chain.  Sites another chain
-// waits for are written to t / elev / bas directly and published through td_done.
+// One warp per chain, bottom to leaf: t_v = 0 + (t_parent + w_v) (below a root t is
+// never -0.0, so that is t_parent + w_v).  Rounds of 32 slots as in the bottom-up
+// walk.  Without slope limits only t is carried (tl, layout order; elevations follow
+// in k_s_finish); with them lane 0 carries the elevation and its clamp too.  The
+// chain's basin outlet and its t / elevation are stored per chain.  Sites another
+// chain waits for are written to t / elev / bas directly and published.
 __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
                              const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
                              const double* __restrict__ wl, const uint8_t* __restrict__ needl,
@@ -616,124 +635,135 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
                              uint32_t* __restrict__ cbas, double* __restrict__ cto,
                              double* __restrict__ ceo, bool slope, int* td_done, int stamp,
                              uint32_t* meta) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= meta[kMetaChains] || td.flags[kError]) return;
+    __shared__ double sw[kWalkWarps][2][32];
+    const int lane = threadIdx.x & 31;
+    const int wb = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * kWalkWarps + wb;
+    // warp-uniform exits only: the warp shuffles with the full mask below
+    if (c >= meta[kMetaChains] || __any_sync(kFull, ld_acquire(&td.flags[kError]) != 0)) return;
     const uint32_t off = coff[c], len = clen[c];
     if (off + len > meta[kMetaNs] || len == 0) {
-        set_error(td.flags, kErrForest);
+        if (lane == 0) set_error(td.flags, kErrForest);
         return;
     }
+    const uint32_t end = off + len;
+    // chain start (lane 0), then broadcast
     uint32_t v = layout[off];
     uint32_t p = td.next[v];
-    double tp, ep, to = 0.0, eo = 0.0;
+    double tp = 0.0, ep = 0.0, to = 0.0, eo = 0.0;
     uint32_t o = kNone;
     uint32_t q = off;
     bool changed = false;
-    if (p == v) {                         // the chain starts at a root
-        double e;
-        tp = settle(td, v, p, 0.0, kNone, 0.0, 0.0, 0.0, &e, &changed);
-        ep = e;
-        o = td.outlet[v] ? v : kNone;
-        to = tp;
-        eo = e;
-        tl[q] = tp;
-        if (slope) el[q] = e;
-        if (needl[q]) {
-            __threadfence();
-            st_release(&td_done[v], stamp);
-        }
-        ++q;
-    } else {
-        uint32_t spins = 0;
-        while (ld_acquire(&td_done[p]) != stamp) {
-            if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
-                set_error(td.flags, kErrWait);
-                return;
-            }
-            __nanosleep(32);
-        }
-        if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
-        tp = __ldcg(&td.t[p]);
-        ep = __ldcg(&td.elev[p]);
-        o = __ldcg(&td.bas[p]);
-        if (o != kNone) {
-            to = __ldcg(&td.t[o]);
-            eo = __ldcg(&td.elev[o]);
-        }
-    }
-    cbas[c] = o;
-    cto[c] = to;
-    ceo[c] = eo;
-    const uint32_t end = off + len;
-    if (!slope) {
-        double bw[kBatch];
-        uint8_t bn[kBatch];
-#pragma unroll
-        for (int i = 0; i < kBatch; ++i) {
-            if (q + i < end) {
-                bw[i] = wl[q + i];
-                bn[i] = needl[q + i];
-            }
-        }
-        while (q < end) {
-            double nw[kBatch];
-            uint8_t nn[kBatch];
-            if (q + 4 * kBatch < end) {
-                prefetch_l1(wl + q + 4 * kBatch);
-                prefetch_l1(wl + q + 5 * kBatch - 1);
-                prefetch_l1(needl + q + 4 * kBatch);
-            }
-#pragma unroll
-            for (int i = 0; i < kBatch; ++i) {
-                if (q + kBatch + i < end) {
-                    nw[i] = wl[q + kBatch + i];
-                    nn[i] = needl[q + kBatch + i];
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < kBatch; ++i) {
-                if (q + i >= end) break;
-                // below a root t is never -0.0, so 0 + (t_p + w) is just t_p + w
-                tp = __dadd_rn(tp, bw[i]);
-                tl[q + i] = tp;
-                if (bn[i]) {                   // another chain hangs here: publish t, elev, bas
-                    uint32_t u = layout[q + i];
-                    double e = __ldcg(&td.elev[u]);
-                    if (o != kNone) {
-                        double dt = __dsub_rn(tp, to);
-                        e = __dadd_rn(eo, __dmul_rn(td.uu[u], dt > 0.0 ? dt : 0.0));
-                        if (e != __ldcg(&td.elev[u])) changed = true;
-                    }
-                    td.t[u] = tp;
-                    td.elev[u] = e;
-                    td.bas[u] = o;
-                    __threadfence();
-                    st_release(&td_done[u], stamp);
-                }
-            }
-            q += kBatch;
-#pragma unroll
-            for (int i = 0; i < kBatch; ++i) {
-                bw[i] = nw[i];
-                bn[i] = nn[i];
-            }
-        }
-    } else {
-        for (; q < end; ++q) {
-            v = layout[q];
+    bool failed = false;
+    if (lane == 0) {
+        if (p == v) {                     // the chain starts at a root
             double e;
-            tp = settle(td, v, p, tp, o, to, eo, ep, &e, &changed);
-            tl[q] = tp;
-            el[q] = e;
+            tp = settle(td, v, p, 0.0, kNone, 0.0, 0.0, 0.0, &e, &changed);
             ep = e;
-            p = v;
+            o = td.outlet[v] ? v : kNone;
+            to = tp;
+            eo = e;
+            tl[q] = tp;
+            if (slope) el[q] = e;
             if (needl[q]) {
                 __threadfence();
                 st_release(&td_done[v], stamp);
             }
+        } else {
+            uint32_t spins = 0;
+            while (ld_acquire(&td_done[p]) != stamp) {
+                if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
+                    set_error(td.flags, kErrWait);
+                    failed = true;
+                    break;
+                }
+                __nanosleep(32);
+            }
+            if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
+            if (!failed) {
+                tp = __ldcg(&td.t[p]);
+                ep = __ldcg(&td.elev[p]);
+                o = __ldcg(&td.bas[p]);
+                if (o != kNone) {
+                    to = __ldcg(&td.t[o]);
+                    eo = __ldcg(&td.elev[o]);
+                }
+            }
         }
+        cbas[c] = o;
+        cto[c] = to;
+        ceo[c] = eo;
     }
-    if (changed) td.flags[kChanged] = 1;
+    if (__shfl_sync(kFull, failed, 0)) return;
+    if (p == v) q = off + 1;
+    tp = __shfl_sync(kFull, tp, 0);
+    ep = __shfl_sync(kFull, ep, 0);
+    o = __shfl_sync(kFull, o, 0);
+    to = __shfl_sync(kFull, to, 0);
+    eo = __shfl_sync(kFull, eo, 0);
+    if (slope) {
+        // lane 0 carries the elevation clamp site by site
+        if (lane == 0) {
+            for (; q < end; ++q) {
+                v = layout[q];
+                double e;
+                tp = settle(td, v, p, tp, o, to, eo, ep, &e, &changed);
+                tl[q] = tp;
+                el[q] = e;
+                ep = e;
+                p = v;
+                if (needl[q]) {
+                    __threadfence();
+                    st_release(&td_done[v], stamp);
+                }
+            }
+            if (changed) td.flags[kChanged] = 1;
+        }
+        return;
+    }
+    double rw = 0.0;
+    uint8_t rn = 0;
+    if (q + lane < end) {
+        rw = wl[q + lane];
+        rn = needl[q + lane];
+    }
+    int cur = 0;
+    for (; q < end; q += 32) {
+        sw[wb][cur][lane] = rw;
+        const uint8_t need = rn;
+        __syncwarp();
+        if (q + 32 + lane < end) {                 // next round in flight
+            rw = wl[q + 32 + lane];
+            rn = needl[q + 32 + lane];
+        }
+        const int cnt = (end - q) < 32u ? (int)(end - q) : 32;
+        double mine = 0.0;
+        for (int i = 0; i < cnt; ++i) {
+            tp = __dadd_rn(tp, sw[wb][cur][i]);
+            if (lane == i) mine = tp;
+        }
+        if (lane < cnt) {
+            tl[q + lane] = mine;
+            if (need) {                             // another chain hangs here: publish
+                uint32_t u = layout[q + lane];
+                double old_e = __ldcg(&td.elev[u]);
+                double e = old_e;
+                if (o != kNone) {
+                    double dt = __dsub_rn(mine, to);
+                    e = __dadd_rn(eo, __dmul_rn(td.uu[u], dt > 0.0 ? dt : 0.0));
+                    if (e != old_e) changed = true;
+                }
+                td.t[u] = mine;
+                td.elev[u] = e;
+                td.bas[u] = o;
+                __threadfence();
+                st_release(&td_done[u], stamp);
+            }
+        }
+        cur ^= 1;
+        __syncwarp();
+    }
+    if (__any_sync(kFull, changed) && lane == 0) td.flags[kChanged] = 1;
 }
 
 // Skeleton response times and elevations back to site order.
@@ -822,13 +852,23 @@ constexpr unsigned kRoundBlock = 1024;
 
 }  // namespace
 
+uint32_t walk_capacity() {
+    int dev = 0, sms = 0, up = 0, down = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&up, k_s_bottom_up, kWalkWarps * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&down, k_s_top_down, kWalkWarps * 32, 0);
+    int per = std::max(1, std::min(up, down));
+    return (uint32_t)(sms * per * kWalkWarps);
+}
+
 cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz) {
     const uint32_t n = a.n;
     const unsigned nb = (n + kThreads - 1) / kThreads;
     const unsigned g_kahn = coop_grid((const void*)k_kahn, kRoundBlock, 2);
     const unsigned g_rank = coop_grid((const void*)k_s_rank, kRoundBlock, 2);
     const unsigned g_low = coop_grid((const void*)k_low_top_down, kRoundBlock, 2);
-    const unsigned g_chain = (a.kahn_min_width + kThreads - 1) / kThreads;
+    const unsigned g_chain = (a.kahn_min_width + kWalkWarps - 1) / kWalkWarps;
     const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
     TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.t, a.elev, a.bas, a.flags};
@@ -880,7 +920,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
 
     // chain walk bottom-up; results in layout order (in place over `pre`)
     hk.begin(hk.ctx);
-    e = coop_launch(k_s_bottom_up, g_chain, kThreads, st, a.row, a.col, a.next,
+    e = coop_launch(k_s_bottom_up, g_chain, kWalkWarps * 32, st, a.row, a.col, a.next,
                     (const uint32_t*)a.hgt, a.area, a.A, (const uint32_t*)a.layout,
                     (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const double*)a.pre,
                     (const double*)a.post, (const double*)a.post1, (const double*)a.post2,
@@ -903,7 +943,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     hk.end(hk.ctx, kcBasinBuild, 0.0);
 
     hk.begin(hk.ctx);
-    e = coop_launch(k_s_top_down, g_chain, kThreads, st, td, (const uint32_t*)a.layout,
+    e = coop_launch(k_s_top_down, g_chain, kWalkWarps * 32, st, td, (const uint32_t*)a.layout,
                     (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const double*)a.post,
                     (const uint8_t*)a.sflag, a.pre, a.el, a.cbas, a.cto, a.ceo, a.slope,
                     a.td_done, a.stamp, a.meta);

@@ -21,6 +21,13 @@ enum KClass {
     kcCount
 };
 
+// Skeleton chains are walked one warp each, this many warps per block.
+constexpr int kWalkWarps = 4;
+
+// Largest skeleton chain count whose walk kernels are all co-resident on the
+// current device (one warp per chain).
+uint32_t walk_capacity();
+
 // Device-side bookkeeping words of one basin pass (uint32 slots of BasinArgs::meta).
 enum Meta {
     kMetaLeaves = 0,   // number of leaves (Kahn round 0)

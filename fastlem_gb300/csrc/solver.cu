@@ -366,6 +366,8 @@ void kresolve(fl_graph* g) {
 
 int alloc_workspace(fl_graph* g) {
     const uint32_t n = g->n;
+    // the Kahn rounds stop once fewer sites are ready than walk warps fit on the GPU
+    g->kahn_min_width = std::min<uint32_t>(kKahnMinWidth, std::max<uint32_t>(256, fl::walk_capacity()));
     FL_TRY(dalloc(&g->d_k, n));
     FL_TRY(dalloc(&g->d_u, n));
     FL_TRY(dalloc(&g->d_tan, n));
