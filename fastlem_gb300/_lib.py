@@ -29,7 +29,7 @@ EXPORTS = [
     "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
-    "fl_graph_basin_stats",
+    "fl_graph_basin_stats", "fl_basin_labels_noalloc",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
     "fl_probe_rng_f64", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
 ]
@@ -71,6 +71,7 @@ def lib():
     L.fl_num_kernel_classes.restype = c_u32
     L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
     L.fl_graph_basin_stats.argtypes = [vp, vp, c_u32]
+    L.fl_basin_labels_noalloc.argtypes = [c_u32, vp, vp, vp, P(c_int), vp]
     L.fl_probe_receivers.argtypes = [vp, vp, vp, vp, P(c_int)]
     L.fl_probe_lakes.argtypes = [vp, vp, c_u32, vp, vp, vp]
     L.fl_probe_tree_pass.argtypes = [vp, vp, c_u32, vp, vp, vp, vp, vp, vp, vp, P(c_int)]

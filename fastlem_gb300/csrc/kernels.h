@@ -111,6 +111,9 @@ struct Hooks {
     void (*end)(void* ctx, int cls, double bytes);
 };
 
+// Sets the message fl_last_error() returns on this thread.
+void set_last_error(const char* msg);
+
 void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const uint32_t* col,
                       const double* len, const double* elev, const uint8_t* outlet,
                       uint32_t* next, double* rlen, int* flags);

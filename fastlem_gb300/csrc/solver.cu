@@ -222,6 +222,10 @@ __global__ void k_fill_f64(uint32_t n, double* __restrict__ a, const double* __r
 
 }  // namespace
 
+namespace fl {
+void set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+}  // namespace fl
+
 // ---------------------------------------------------------------------------
 // Model handle
 // ---------------------------------------------------------------------------

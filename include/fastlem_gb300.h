@@ -145,6 +145,25 @@ int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
  * starting at sample `first` (the initial-elevation noise of lem/generator.rs:134-138). */
 int fl_probe_rng_f64(uint64_t seed, uint64_t first, uint64_t count, double* out);
 
+/* ---- allocation-free variant ----------------------------------------------------- */
+
+/* Basin labels (the root every site drains to, lem/stream_tree.rs:139-173) and
+ * has_lake, for callers that must not allocate device memory -- e.g. a service whose
+ * device memory comes from its own fixed pool, where a cudaMalloc would escape the
+ * pool's accounting and synchronise the device.  No counterpart in the reference:
+ * fastlem computes labels inside StreamTree::construct.
+ *   next, outlet_table: device arrays of n entries (receivers; nonzero = outlet)
+ *   labels:             device array of n entries, written
+ *   has_lake:           host int (may be NULL)
+ *   stream:             cudaStream_t (NULL = default stream)
+ * Allocates nothing: the only scratch is a fixed 16 MiB device array inside the
+ * library, held by every GPU that loads it, so n must not exceed 4,194,304
+ * (FL_ERR_INVALID_ARGUMENT otherwise).  The first call on a device looks up that
+ * array's address; make it before any stream capture.  Calls share the scratch, so
+ * calls that overlap on one GPU race: serialise them. */
+int fl_basin_labels_noalloc(uint32_t n, const uint32_t* next, const uint8_t* outlet_table,
+                            uint32_t* labels, int* has_lake, void* stream);
+
 /* ---- host model builder (models/surface/builder.rs) ------------------------------ */
 
 /* `from_random_sites` sampler (builder.rs:38-52): x = gen_range(x0..x1), then
