@@ -31,7 +31,7 @@ EXPORTS = [
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_basin_labels_noalloc",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
-    "fl_probe_rng_f64", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
+    "fl_probe_rng_f64", "fl_probe_chain_fold", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
 ]
 
 c_u32, c_u64, c_int, c_dbl, vp = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
@@ -77,6 +77,7 @@ def lib():
     L.fl_probe_tree_pass.argtypes = [vp, vp, c_u32, vp, vp, vp, vp, vp, vp, vp, P(c_int)]
     L.fl_probe_prim_rank.argtypes = [vp, vp, c_u32, vp]
     L.fl_probe_rng_f64.argtypes = [c_u64, c_u64, c_u64, vp]
+    L.fl_probe_chain_fold.argtypes = [vp, c_u32, c_dbl, vp]
     L.fl_random_sites.argtypes = [c_u64, c_dbl, c_dbl, c_dbl, c_dbl, c_u64, c_int, vp, vp]
     L.fl_relax_sites.argtypes = [c_u32, vp, vp, c_dbl, c_dbl, c_dbl, c_dbl, c_u32]
     L.fl_build_graph.argtypes = [c_u32, vp, vp, c_dbl, c_dbl, c_dbl, c_dbl, vp, vp, vp, c_u64,

@@ -23,7 +23,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_SOURCES = ["solver.cu", "receivers.cu", "basin.cu", "noalloc.cu"]
 CXX_SOURCES = ["builder.cpp", "prim_rank.cpp", "ordering.cpp"]
-HEADERS = ["rng.h", "common.cuh", "kernels.h"]
+HEADERS = ["rng.h", "common.cuh", "kernels.h", "fold.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xptxas", "-v",

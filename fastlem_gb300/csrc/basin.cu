@@ -35,6 +35,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "fold.cuh"
 #include "kernels.h"
 
 namespace fl {
@@ -454,11 +455,12 @@ __device__ double warp_slow_pull(uint32_t v, uint32_t heavy, double x,
     return acc;
 }
 
-// One warp per chain, leaf to bottom.  Each round the lanes load 32 slots (coalesced)
-// into shared memory and issue the next 32 slots' loads; then every lane replays the
-// 32 dependent additions (identical, so branches are warp-uniform) and lane i keeps
-// the result of slot i.  Results go to Al (layout order); the chain bottom's area is
-// also stored in A and published through bu_done.
+// One warp per chain, leaf to bottom.  Each round the lanes load 32 slots (lane l the
+// slot l places below the round's top, coalesced) and issue the next round's loads;
+// warp_fold then applies every slot's additions to the running area exactly (integer
+// scan between binade crossings and ties, f64 additions for those).  Chain leaves and
+// confluences are evaluated one at a time.  Results go to Al (layout order); the chain
+// bottom's area is also stored in A and published through bu_done.
 __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
                               const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
                               const double* __restrict__ area, double* A,
@@ -468,8 +470,6 @@ __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* 
                               const double* __restrict__ post1, const double* __restrict__ post2,
                               const uint8_t* __restrict__ sflag, double* __restrict__ Al,
                               int* bu_done, int stamp, uint32_t* meta, int* flags) {
-    __shared__ double sv[kWalkWarps][2][4][32];
-    __shared__ uint8_t sf[kWalkWarps][2][32];
     const int lane = threadIdx.x & 31;
     const int wb = threadIdx.x >> 5;
     const uint32_t c = blockIdx.x * kWalkWarps + wb;
@@ -483,54 +483,45 @@ __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* 
     }
     const int64_t lo = off;
     int64_t top = (int64_t)off + len - 1;
-    double rp = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0;
-    uint8_t rf = 0;
-    auto load = [&](int64_t t) {
+    double y[kFoldOps] = {0.0, 0.0, 0.0, 0.0};
+    uint8_t f = 0;
+    auto load = [&](int64_t t, double (&dst)[kFoldOps], uint8_t& fl_) {
         int64_t q = t - lane;
         if (q >= lo) {
-            rp = pre[q];
-            r0 = post[q];
-            r1 = post1[q];
-            r2 = post2[q];
-            rf = sflag[q];
+            dst[0] = pre[q];
+            dst[1] = post[q];
+            dst[2] = post1[q];
+            dst[3] = post2[q];
+            fl_ = sflag[q];
         }
     };
-    load(top);
+    load(top, y, f);
     double x = 0.0;
     bool ok = true;
     uint32_t spins = 0;
-    int cur = 0;
     for (; top >= lo; top -= 32) {
-        sv[wb][cur][0][lane] = rp;
-        sv[wb][cur][1][lane] = r0;
-        sv[wb][cur][2][lane] = r1;
-        sv[wb][cur][3][lane] = r2;
-        sf[wb][cur][lane] = rf;
-        __syncwarp();
-        load(top - 32);                               // next round in flight
+        double ny[kFoldOps] = {0.0, 0.0, 0.0, 0.0};
+        uint8_t nf = 0;
+        load(top - 32, ny, nf);                       // next round in flight
         const int64_t left = top - lo + 1;
         const int cnt = left < 32 ? (int)left : 32;
+        const bool special = (f & (kLeafSlot | kSlow)) != 0;
+        const int nop = 1 + ((f >> kPostShift) & 3);
+        const int64_t t0 = top;
         double mine = 0.0;
-        for (int i = 0; i < cnt; ++i) {
-            const uint8_t f = sf[wb][cur][i];
-            if (f & kLeafSlot) {
-                x = sv[wb][cur][0][i];
-            } else if (!(f & kSlow)) {
-                const int np = (f >> kPostShift) & 3;
-                x = __dadd_rn(sv[wb][cur][0][i], x);
-                if (np > 0) x = __dadd_rn(x, sv[wb][cur][1][i]);
-                if (np > 1) x = __dadd_rn(x, sv[wb][cur][2][i]);
-                if (np > 2) x = __dadd_rn(x, sv[wb][cur][3][i]);
-            } else {
-                x = warp_slow_pull(layout[top - i], layout[top - i + 1], x, row, col, next, hgt,
-                                   area, A, bu_done, stamp, flags, &ok, &spins);
-                if (!ok) return;
-            }
-            if (lane == i) mine = x;
-        }
+        x = warp_fold(x, y, nop, special, cnt, mine, [&](int k, double xin) -> double {
+            const uint8_t fk = (uint8_t)__shfl_sync(kFull, (uint32_t)f, k);
+            const double pk = __shfl_sync(kFull, y[0], k);
+            if (fk & kLeafSlot) return pk;             // chain leaf: its own complete pull
+            if (!ok) return xin;
+            return warp_slow_pull(layout[t0 - k], layout[t0 - k + 1], xin, row, col, next, hgt,
+                                  area, A, bu_done, stamp, flags, &ok, &spins);
+        });
+        if (!ok) return;
         if (lane < cnt) Al[top - lane] = mine;
-        cur ^= 1;
-        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < kFoldOps; ++j) y[j] = ny[j];
+        f = nf;
     }
     if (lane == 0) {
         uint32_t bottom = layout[off];
@@ -635,7 +626,6 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
                              uint32_t* __restrict__ cbas, double* __restrict__ cto,
                              double* __restrict__ ceo, bool slope, int* td_done, int stamp,
                              uint32_t* meta) {
-    __shared__ double sw[kWalkWarps][2][32];
     const int lane = threadIdx.x & 31;
     const int wb = threadIdx.x >> 5;
     const uint32_t c = blockIdx.x * kWalkWarps + wb;
@@ -727,21 +717,18 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
         rw = wl[q + lane];
         rn = needl[q + lane];
     }
-    int cur = 0;
     for (; q < end; q += 32) {
-        sw[wb][cur][lane] = rw;
+        const double wv = rw;
         const uint8_t need = rn;
-        __syncwarp();
         if (q + 32 + lane < end) {                 // next round in flight
             rw = wl[q + 32 + lane];
             rn = needl[q + 32 + lane];
         }
         const int cnt = (end - q) < 32u ? (int)(end - q) : 32;
         double mine = 0.0;
-        for (int i = 0; i < cnt; ++i) {
-            tp = __dadd_rn(tp, sw[wb][cur][i]);
-            if (lane == i) mine = tp;
-        }
+        const double yv[kFoldOps] = {wv, 0.0, 0.0, 0.0};
+        tp = warp_fold(tp, yv, 1, false, cnt, mine,
+                       [](int, double xin) -> double { return xin; });
         if (lane < cnt) {
             tl[q + lane] = mine;
             if (need) {                             // another chain hangs here: publish
@@ -760,8 +747,6 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
                 st_release(&td_done[u], stamp);
             }
         }
-        cur ^= 1;
-        __syncwarp();
     }
     if (__any_sync(kFull, changed) && lane == 0) td.flags[kChanged] = 1;
 }
@@ -851,6 +836,25 @@ unsigned coop_grid(const void* kernel, unsigned block, unsigned cap_per_sm) {
 constexpr unsigned kRoundBlock = 1024;
 
 }  // namespace
+
+// Probe: x_k after each operand of one chain (one operand per slot), by warp_fold.
+__global__ void k_fold_probe(const double* __restrict__ y, uint32_t n, double x0,
+                             double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    double x = x0;
+    for (uint32_t base = 0; base < n; base += 32) {
+        const int cnt = (n - base) < 32u ? (int)(n - base) : 32;
+        const double yv[kFoldOps] = {base + lane < n ? y[base + lane] : 0.0, 0.0, 0.0, 0.0};
+        double mine = 0.0;
+        x = warp_fold(x, yv, 1, false, cnt, mine, [](int, double xin) -> double { return xin; });
+        if (lane < cnt) out[base + lane] = mine;
+    }
+}
+
+cudaError_t fold_probe(const double* y, uint32_t n, double x0, double* out) {
+    k_fold_probe<<<1, 32>>>(y, n, x0, out);
+    return cudaGetLastError();
+}
 
 uint32_t walk_capacity() {
     int dev = 0, sms = 0, up = 0, down = 0;

@@ -118,6 +118,9 @@ void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const ui
                       const double* len, const double* elev, const uint8_t* outlet,
                       uint32_t* next, double* rlen, int* flags);
 
+// Runs the exact parallel fold over one chain of n operands starting at x0 (probe).
+cudaError_t fold_probe(const double* y, uint32_t n, double x0, double* out);
+
 // One drainage-area / response-time / elevation pass on final receivers.
 cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz);
 

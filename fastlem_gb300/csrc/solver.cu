@@ -937,6 +937,20 @@ int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     return FL_OK;
 }
 
+int fl_probe_chain_fold(const double* operands, uint32_t n, double start, double* out) {
+    double* d = nullptr;
+    FL_CU(cudaMalloc(&d, std::max<uint64_t>(1, 2ull * n) * 8));
+    cudaError_t e = cudaMemcpy(d, operands, n * 8ull, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = fl::fold_probe(d, n, start, d + n);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + n, n * 8ull, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        set_err("fl_probe_chain_fold", e);
+        return FL_ERR_CUDA;
+    }
+    return FL_OK;
+}
+
 int fl_select_device(int device) {
     FL_CU(cudaSetDevice(device));
     return FL_OK;

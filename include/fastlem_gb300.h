@@ -141,6 +141,11 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
  * (lem/stream_tree.rs:184-240), computed on the host: rank[v], UINT32_MAX if never. */
 int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets, uint32_t* rank);
 
+/* x_k = (...((start + op_0) + op_1) ... + op_k) with every addition rounded, as the
+ * reference's sequential accumulations do, evaluated by the solver's parallel exact
+ * fold (the chain walks' arithmetic). */
+int fl_probe_chain_fold(const double* operands, uint32_t n, double start, double* out);
+
 /* `count` samples of StdRng::seed_from_u64(seed).gen::<f64>() drawn on the device,
  * starting at sample `first` (the initial-elevation noise of lem/generator.rs:134-138). */
 int fl_probe_rng_f64(uint64_t seed, uint64_t first, uint64_t count, double* out);
