@@ -246,10 +246,17 @@ def bench_gpu(args, d):
     dname, (dl, dms, dbytes) = dom
     peak, peak_kind = peak_hbm()
     achieved = (dbytes / dl) / ((dms / dl) / 1000) / 1e9 if dl and dms else 0.0
+    all_bytes = sum(v[2] for v in stats.values())
+    all_ms = sum(v[1] for v in stats.values())
     roof = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
             "bytes_per_launch": dbytes / max(1, dl), "ms_per_launch": dms / max(1, dl),
-            "launches": dl}
+            "launches": dl,
+            # every kernel class together: algorithmic bytes of the whole solve over its
+            # device time
+            "all_kernels": {"achieved": all_bytes / (all_ms / 1000) / 1e9 if all_ms else 0.0,
+                            "frac": (all_bytes / (all_ms / 1000) / 1e9 / peak) if all_ms else 0.0,
+                            "bytes_per_iteration": all_bytes / max(1, iters)}}
     share = {k: round(v[1] / max(1e-9, sum(x[1] for x in stats.values())), 4)
              for k, v in stats.items() if v[0]}
     cpu = None

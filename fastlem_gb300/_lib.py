@@ -29,7 +29,7 @@ EXPORTS = [
     "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
-    "fl_graph_basin_stats", "fl_basin_labels_noalloc",
+    "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
     "fl_probe_rng_f64", "fl_probe_chain_fold", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
 ]
@@ -71,6 +71,7 @@ def lib():
     L.fl_num_kernel_classes.restype = c_u32
     L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
     L.fl_graph_basin_stats.argtypes = [vp, vp, c_u32]
+    L.fl_graph_round_trace.argtypes = [vp, c_u32, P(c_u32), vp, vp, vp]
     L.fl_basin_labels_noalloc.argtypes = [c_u32, vp, vp, vp, P(c_int), vp]
     L.fl_probe_receivers.argtypes = [vp, vp, vp, vp, P(c_int)]
     L.fl_probe_lakes.argtypes = [vp, vp, c_u32, vp, vp, vp]
@@ -134,7 +135,9 @@ def kernel_stats(handle):
 
 
 BASIN_STATS = ["kahn_rounds", "leaves", "skeleton_sites", "chains", "longest_chain", "slow_sites",
-               "wait_spins_up", "wait_spins_down"]
+               "wait_spins_up", "wait_spins_down", "up_slowest_ns", "up_slowest_pull_cycles",
+               "up_slowest_pulls", "down_slowest_ns", "down_slowest_wait_cycles",
+               "down_slowest_len"]
 
 
 def basin_stats(handle):
@@ -142,3 +145,16 @@ def basin_stats(handle):
     out = np.zeros(len(BASIN_STATS), np.uint64)
     check(lib().fl_graph_basin_stats(handle, out.ctypes.data_as(vp), len(BASIN_STATS)))
     return dict(zip(BASIN_STATS, (int(x) for x in out)))
+
+
+def round_trace(handle, cap=1 << 16):
+    """Kahn-round structure of the last basin pass: (offsets, up_ns, down_ns), each
+    of length rounds + 1 (device clock in ns; see fl_graph_round_trace)."""
+    r = ctypes.c_uint32(0)
+    off = np.zeros(cap, np.uint32)
+    up = np.zeros(cap, np.uint64)
+    down = np.zeros(cap, np.uint64)
+    check(lib().fl_graph_round_trace(handle, cap, ctypes.byref(r), off.ctypes.data_as(vp),
+                                     up.ctypes.data_as(vp), down.ctypes.data_as(vp)))
+    k = min(cap, r.value + 1)
+    return off[:k], up[:k], down[:k]

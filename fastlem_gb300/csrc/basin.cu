@@ -99,12 +99,12 @@ __global__ void k_count_donors(uint32_t n, const uint32_t* __restrict__ next,
     if (p != v) atomicAdd(&pending[p], 1u);
 }
 
+// Leaves in site order per block range (one reservation per block).
 __global__ void k_collect_leaves(uint32_t n, const uint32_t* __restrict__ pending,
                                  uint32_t* __restrict__ order, uint32_t* __restrict__ counter) {
-    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
-    uint32_t pos = warp_append(counter, pending[v] == 0);
-    if (pos != kNone) order[pos] = v;
+    block_range_compact(
+        n, counter, [&](uint32_t v) { return pending[v] == 0; },
+        [&](uint32_t v, uint32_t pos) { order[pos] = v; });
 }
 
 // Kahn rounds.  order[0, nleaves) holds the leaves; rounds append the next frontier
@@ -114,7 +114,8 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
                        const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
                        const double* __restrict__ area, double* A, uint32_t* pending,
                        uint32_t* __restrict__ hgt, uint32_t* order, uint32_t* roff,
-                       uint32_t max_rounds, uint32_t min_width, uint32_t* meta, int* flags) {
+                       uint64_t* __restrict__ rtime, uint32_t max_rounds, uint32_t min_width,
+                       uint32_t* meta, int* flags) {
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t beg = 0, end = ld_acquire_u(&meta[kMetaLeaves]);
@@ -124,18 +125,25 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
         roff[1] = end;
     }
     while (true) {
+        if (gtid == 0) rtime[r] = global_ns();
         uint32_t width = end - beg;
         if (width == 0 || width < min_width || r + 2 >= max_rounds) break;
         uint32_t* cnt = &meta[kMetaCnt0 + (r % 3)];
         if (gtid == 0) meta[kMetaCnt0 + ((r + 1) % 3)] = 0;
-        for (uint32_t idx = beg + gtid; idx < end; idx += stride) {
-            uint32_t v = __ldcg(&order[idx]);
-            // round 0 is the leaves: no donors, the drainage area is the cell area
-            A[v] = (r == 0) ? area[v] : pull_area(v, row, col, next, area, A);
-            hgt[v] = r;
-            uint32_t p = next[v];
-            bool ready = p != v && atomicSub(&pending[p], 1u) == 1u;
-            uint32_t pos = warp_append(cnt, ready);
+        // block-uniform trip count: block_append synchronises the block
+        for (uint32_t tile = beg + blockIdx.x * blockDim.x; tile < end; tile += stride) {
+            const uint32_t idx = tile + threadIdx.x;
+            bool ready = false;
+            uint32_t p = 0;
+            if (idx < end) {
+                uint32_t v = __ldcg(&order[idx]);
+                // round 0 is the leaves: no donors, the drainage area is the cell area
+                A[v] = (r == 0) ? area[v] : pull_area(v, row, col, next, area, A);
+                hgt[v] = r;
+                p = next[v];
+                ready = p != v && atomicSub(&pending[p], 1u) == 1u;
+            }
+            uint32_t pos = block_append(cnt, ready);
             if (pos != kNone) {
                 pos += end;
                 if (pos < n) order[pos] = p;
@@ -168,13 +176,12 @@ struct Ranks {
 __global__ void k_s_collect(uint32_t n, const uint32_t* __restrict__ hgt,
                             uint32_t* __restrict__ sid, uint32_t* __restrict__ slist,
                             uint32_t* meta) {
-    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
-    uint32_t k = warp_append(&meta[kMetaNs], hgt[v] == kNone);
-    if (k != kNone) {
-        sid[v] = k;
-        slist[k] = v;
-    }
+    block_range_compact(
+        n, &meta[kMetaNs], [&](uint32_t v) { return hgt[v] == kNone; },
+        [&](uint32_t v, uint32_t k) {
+            sid[v] = k;
+            slist[k] = v;
+        });
 }
 
 // For skeleton site p: the skeleton donor that continues p's chain (largest
@@ -400,6 +407,16 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
 constexpr int kBatch = 8;
 constexpr unsigned kFull = 0xffffffffu;
 
+// Keeps the slowest chain's walk statistic in meta[slot] (two words).
+__device__ __forceinline__ void record_chain_stat(uint32_t* meta, int slot, uint64_t dur_ns,
+                                                  uint64_t cycles, uint64_t count) {
+    const uint64_t d = dur_ns >> 6, c = cycles >> 7;
+    const uint64_t key = ((d < kStat22 ? d : kStat22) << kStatDurShift) |
+                         ((c < kStat22 ? c : kStat22) << kStatCycShift) |
+                         (count < kStat20 ? count : kStat20);
+    atomicMax((unsigned long long*)&meta[slot], (unsigned long long)key);
+}
+
 // Full pull of v during the walk, by the whole warp: lane l takes slot s1-1-l (reverse
 // row order), the values are folded in lane order.  The chain predecessor's value is
 // x; another skeleton donor is a chain bottom, waited for through bu_done.
@@ -461,7 +478,7 @@ __device__ double warp_slow_pull(uint32_t v, uint32_t heavy, double x,
 // scan between binade crossings and ties, f64 additions for those).  Chain leaves and
 // confluences are evaluated one at a time.  Results go to Al (layout order); the chain
 // bottom's area is also stored in A and published through bu_done.
-__global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
+__global__ void __launch_bounds__(kWalkWarps * 32, 7) k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
                               const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
                               const double* __restrict__ area, double* A,
                               const uint32_t* __restrict__ layout,
@@ -481,6 +498,8 @@ __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* 
         if (lane == 0) set_error(flags, kErrForest);
         return;
     }
+    const uint64_t t_start = global_ns();
+    uint32_t slow_cycles = 0, slow_n = 0;
     const int64_t lo = off;
     int64_t top = (int64_t)off + len - 1;
     double y[kFoldOps] = {0.0, 0.0, 0.0, 0.0};
@@ -514,8 +533,12 @@ __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* 
             const double pk = __shfl_sync(kFull, y[0], k);
             if (fk & kLeafSlot) return pk;             // chain leaf: its own complete pull
             if (!ok) return xin;
-            return warp_slow_pull(layout[t0 - k], layout[t0 - k + 1], xin, row, col, next, hgt,
-                                  area, A, bu_done, stamp, flags, &ok, &spins);
+            const long long c0 = clock64();
+            const double r = warp_slow_pull(layout[t0 - k], layout[t0 - k + 1], xin, row, col,
+                                            next, hgt, area, A, bu_done, stamp, flags, &ok, &spins);
+            slow_cycles += (uint32_t)(clock64() - c0);
+            ++slow_n;
+            return r;
         });
         if (!ok) return;
         if (lane < cnt) Al[top - lane] = mine;
@@ -531,6 +554,7 @@ __global__ void k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* 
     }
     spins = __reduce_add_sync(kFull, spins);
     if (lane == 0 && spins) atomicAdd(&meta[kMetaSpinUp], spins);
+    if (lane == 0) record_chain_stat(meta, kMetaUpSlow, global_ns() - t_start, slow_cycles, slow_n);
 }
 
 // Skeleton areas back to site order.
@@ -661,6 +685,8 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
             }
         } else {
             uint32_t spins = 0;
+            const uint64_t t0 = global_ns();
+            const long long c0 = clock64();
             while (ld_acquire(&td_done[p]) != stamp) {
                 if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
                     set_error(td.flags, kErrWait);
@@ -669,6 +695,8 @@ __global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
                 }
                 __nanosleep(32);
             }
+            // the chain that waited longest for its parent
+            record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
             if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
             if (!failed) {
                 tp = __ldcg(&td.t[p]);
@@ -785,12 +813,14 @@ __global__ void k_s_finish(TopDown td, const uint32_t* __restrict__ layout,
 
 // Top-down over the Kahn rounds, highest round first.
 __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
-                               const uint32_t* __restrict__ roff, const uint32_t* meta) {
+                               const uint32_t* __restrict__ roff, uint64_t* __restrict__ rtime,
+                               const uint32_t* meta) {
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
     if (ld_acquire(&td.flags[kError])) return;
     uint32_t rs = meta[kMetaRStop];
     bool changed = false;
+    if (gtid == 0) rtime[0] = global_ns();
     for (uint32_t r = rs; r-- > 0;) {
         uint32_t b = roff[r], e = roff[r + 1];
         for (uint32_t i = b + gtid; i < e; i += stride) {
@@ -811,6 +841,7 @@ __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
             settle(td, v, p, tp, o, to, eo, ep, &en, &changed);
         }
         if (!grid_barrier(td.flags)) return;
+        if (gtid == 0) rtime[rs - r] = global_ns();
     }
     block_flag(td.flags, kChanged, changed);
 }
@@ -872,6 +903,8 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     const unsigned g_kahn = coop_grid((const void*)k_kahn, kRoundBlock, 2);
     const unsigned g_rank = coop_grid((const void*)k_s_rank, kRoundBlock, 2);
     const unsigned g_low = coop_grid((const void*)k_low_top_down, kRoundBlock, 2);
+    // ordered compactions: one block range each, two blocks per SM
+    const unsigned g_compact = coop_grid((const void*)k_collect_leaves, kRoundBlock, 2);
     const unsigned g_chain = (a.kahn_min_width + kWalkWarps - 1) / kWalkWarps;
     const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
@@ -883,19 +916,20 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     cudaMemsetAsync(a.hgt, 0xff, n * 4ull, st);
     cudaMemsetAsync(a.meta, 0, kMetaCount * 4ull, st);
     k_count_donors<<<nb, kThreads, 0, st>>>(n, a.next, a.pending);
-    k_collect_leaves<<<nb, kThreads, 0, st>>>(n, a.pending, a.order, a.meta + kMetaLeaves);
+    k_collect_leaves<<<g_compact, kRoundBlock, 0, st>>>(n, a.pending, a.order, a.meta + kMetaLeaves);
     hk.end(hk.ctx, kcBasinBuild, 20.0 * n);
 
     // Kahn rounds: order 4 + next 4 + row 8 + area 8 + A 8 + hgt 4 + pending 4 per site,
     // col 4 + next 4 per slot, donor areas 8 per site
     hk.begin(hk.ctx);
     e = coop_launch(k_kahn, g_kahn, kRoundBlock, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
-                    a.hgt, a.order, a.roff, a.max_rounds, a.kahn_min_width, a.meta, a.flags);
+                    a.hgt, a.order, a.roff, a.rtime, a.max_rounds, a.kahn_min_width, a.meta,
+                    a.flags);
     hk.end(hk.ctx, kcKahn, 48.0 * n + 8.0 * nnz);
     if (e != cudaSuccess) return e;
 
     hk.begin(hk.ctx);
-    k_s_collect<<<nb, kThreads, 0, st>>>(n, a.hgt, a.sid, a.slist, a.meta);
+    k_s_collect<<<g_compact, kRoundBlock, 0, st>>>(n, a.hgt, a.sid, a.slist, a.meta);
     k_s_designate<<<gs, kThreads, 0, st>>>(a.row, a.col, a.next, a.hgt, a.A, a.slist, a.desig,
                                            a.meta);
     k_s_link<<<gs, kThreads, 0, st>>>(a.next, a.desig, a.hgt, a.sid, a.slist, a.sptr0, a.sdist0,
@@ -966,7 +1000,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     // parent t/elev/bas 20, outlet t/elev 16 per site
     hk.begin(hk.ctx);
     e = coop_launch(k_low_top_down, g_low, kRoundBlock, st, td, (const uint32_t*)a.order,
-                    (const uint32_t*)a.roff, (const uint32_t*)a.meta);
+                    (const uint32_t*)a.roff, a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta);
     hk.end(hk.ctx, kcLowDown, 112.0 * n);
     return e;
 }

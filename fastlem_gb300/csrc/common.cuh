@@ -111,6 +111,86 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
     return base + (uint32_t)__popc(ballot & ((1u << lane) - 1u));
 }
 
+// Block-wide ordered append: the threads of the block whose pred is set get
+// consecutive slots of *counter in thread order, with one atomicAdd per call (a warp-
+// per-call scheme is limited by same-address atomic throughput on wide frontiers).
+// Returns the thread's slot, or kNone.  Every thread of the block must call it, with
+// blockDim.x a multiple of 32.
+__device__ __forceinline__ uint32_t block_append(uint32_t* counter, bool pred) {
+    __shared__ uint32_t s_cnt[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned ballot = __ballot_sync(0xffffffffu, pred);
+    if (lane == 0) s_cnt[wid] = __popc(ballot);
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        const uint32_t own = lane < nw ? s_cnt[lane] : 0;
+        uint32_t inc = own;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        uint32_t base = 0;
+        if (lane == 31 && inc) base = atomicAdd(counter, inc);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        if (lane < nw) s_cnt[lane] = base + inc - own;
+    }
+    __syncthreads();
+    const uint32_t pos = pred ? s_cnt[wid] + (uint32_t)__popc(ballot & ((1u << lane) - 1u)) : kNone;
+    __syncthreads();
+    return pos;
+}
+
+// Ordered compaction of the indices i in [0, n) with pred(i), with one atomicAdd
+// per block: block b takes a contiguous range, counts it, reserves its slots of
+// *counter and calls emit(i, slot) in index order.  Every thread of the block must
+// call it, with blockDim.x a multiple of 32.
+template <class Pred, class Emit>
+__device__ __forceinline__ void block_range_compact(uint32_t n, uint32_t* counter, Pred pred,
+                                                    Emit emit) {
+    __shared__ uint32_t s_cnt[32];
+    __shared__ uint32_t s_run;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    const uint64_t per = ((uint64_t)n + gridDim.x - 1) / gridDim.x;
+    const uint32_t lo = (uint32_t)(blockIdx.x * per < n ? blockIdx.x * per : n);
+    const uint32_t hi = (uint32_t)((blockIdx.x + 1) * per < n ? (blockIdx.x + 1) * per : n);
+    uint32_t c = 0;
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) c += pred(i) ? 1u : 0u;
+    c = __reduce_add_sync(0xffffffffu, c);
+    if (lane == 0) s_cnt[wid] = c;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t t = lane < nw ? s_cnt[lane] : 0;
+        t = __reduce_add_sync(0xffffffffu, t);
+        if (lane == 0) s_run = t ? atomicAdd(counter, t) : 0;
+    }
+    __syncthreads();
+    for (uint32_t tile = lo; tile < hi; tile += blockDim.x) {
+        const uint32_t i = tile + threadIdx.x;
+        const bool p = i < hi && pred(i);
+        const unsigned ballot = __ballot_sync(0xffffffffu, p);
+        if (lane == 0) s_cnt[wid] = __popc(ballot);
+        __syncthreads();
+        if (wid == 0) {
+            const uint32_t own = lane < nw ? s_cnt[lane] : 0;
+            uint32_t inc = own;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += t;
+            }
+            const uint32_t run = s_run;
+            if (lane < nw) s_cnt[lane] = run + inc - own;
+            if (lane == 31) s_run = run + inc;
+        }
+        __syncthreads();
+        if (p) emit(i, s_cnt[wid] + (uint32_t)__popc(ballot & ((1u << lane) - 1u)));
+        __syncthreads();
+    }
+}
+
 // Raises flags[slot] once per block if any thread's pred is set.  Every thread of
 // the block must call it (it contains __syncthreads).
 __device__ __forceinline__ void block_flag(int* flags, int slot, bool pred) {
@@ -119,5 +199,12 @@ __device__ __forceinline__ void block_flag(int* flags, int slot, bool pred) {
 
 // `0.0 + x` exactly as IEEE evaluates it: x itself, except that -0.0 becomes +0.0.
 __device__ __forceinline__ double plus_zero(double x) { return x == 0.0 ? 0.0 : x; }
+
+// Nanosecond wall clock shared by all SMs (instrumentation).
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 }  // namespace fl

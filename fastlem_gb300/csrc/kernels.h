@@ -47,8 +47,21 @@ enum Meta {
     kMetaSpinUp,       // wait iterations of the bottom-up chain hand-offs
     kMetaSpinDown,     // wait iterations of the top-down chain hand-offs
     kMetaMaxChain,     // longest skeleton chain
+    kMetaPad,
+    kMetaUpSlow,       // (2 words, u64) slowest bottom-up chain, packed by pack_chain_stat
+    kMetaUpSlowHi,
+    kMetaDownSlow,     // (2 words, u64) slowest top-down chain, packed by pack_chain_stat
+    kMetaDownSlowHi,
     kMetaCount
 };
+static_assert(kMetaUpSlow % 2 == 0 && kMetaDownSlow % 2 == 0, "u64 meta words must be aligned");
+
+// Per-chain walk statistic packed for atomicMax: duration / 64 ns (22 bits), a cycle
+// count / 128 (22 bits), a count (20 bits).  The largest key is the slowest chain.
+constexpr int kStatDurShift = 42;
+constexpr int kStatCycShift = 20;
+constexpr uint64_t kStat22 = (1ull << 22) - 1;
+constexpr uint64_t kStat20 = (1ull << 20) - 1;
 
 struct BasinArgs {
     uint32_t n;
@@ -70,6 +83,8 @@ struct BasinArgs {
     uint32_t* hgt;
     uint32_t* order;
     uint32_t* roff;
+    uint64_t* rtime;           // globaltimer at the start of each round: Kahn rounds at
+                               // [0, max_rounds], top-down rounds after them
     uint32_t max_rounds;
     uint32_t kahn_min_width;   // also the chain capacity
     uint32_t* meta;

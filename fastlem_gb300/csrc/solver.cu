@@ -263,6 +263,7 @@ struct fl_graph {
     unsigned long long* d_best = nullptr;
     int* d_flags = nullptr;
     // basin pass workspace (device)
+    uint64_t* d_rtime = nullptr;
     uint32_t *d_pending = nullptr, *d_hgt = nullptr, *d_order = nullptr, *d_roff = nullptr,
              *d_meta = nullptr, *d_sid = nullptr, *d_slist = nullptr, *d_desig = nullptr,
              *d_sptr0 = nullptr, *d_sdist0 = nullptr, *d_sptr1 = nullptr, *d_sdist1 = nullptr,
@@ -304,7 +305,7 @@ void free_graph(fl_graph* g) {
                     g->d_sdist1, g->d_cid, g->d_cbot, g->d_clen, g->d_coff, g->d_layout,
                     g->d_pre, g->d_post, g->d_sflag, g->d_bu_done, g->d_td_need, g->d_td_done,
                     g->d_slot_chain, g->d_cbas, g->d_el, g->d_cto, g->d_ceo, g->d_perm, g->d_inv,
-                    g->d_post1, g->d_post2};
+                    g->d_post1, g->d_post2, g->d_rtime};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -397,6 +398,7 @@ int alloc_workspace(fl_graph* g) {
     // each Kahn round retires at least kahn_min_width sites
     g->max_rounds = n / g->kahn_min_width + 64;
     FL_TRY(dalloc(&g->d_roff, g->max_rounds + 2));
+    FL_TRY(dalloc(&g->d_rtime, 2ull * (g->max_rounds + 1)));
     FL_TRY(dalloc(&g->d_meta, kMetaCount));
     FL_TRY(dalloc(&g->d_sid, n));
     FL_TRY(dalloc(&g->d_slist, n));
@@ -580,6 +582,26 @@ int run_lakes(fl_graph* g) {
 }
 
 // Drainage areas, response times, elevations on final receivers; *changed.
+// Algorithmic bytes of the kernels that work on the skeleton, whose size is known
+// only once the pass has run (the launch groups were counted with 0 bytes).
+//   bottom-up: pre, post, post1, post2 (32) + flags (1) + area out (8) per slot;
+//              offset, length, bottom id, bottom area, hand-off flag (24) per chain
+//   top-down:  w (8) + flags (1) + t out (8) [+ elevation out (8) with slope limits]
+//              per slot; offset, length, parent t / elevation / outlet, chain outlet
+//              t / elevation / id out (56) per chain
+//   ranking:   per pointer-jumping round, own and successor's pointer and distance
+//              in (16) and out (8) per skeleton site; ceil(log2(longest chain)) + 1
+//              rounds
+void account_skeleton(fl_graph* g) {
+    const double ns = g->last_meta[kMetaNs], nc = g->last_meta[kMetaChains];
+    const uint32_t longest = g->last_meta[kMetaMaxChain];
+    int rounds = 1;
+    while (rounds < 32 && (1u << (rounds - 1)) < longest) ++rounds;
+    g->k_bytes[kcSkelUp] += 41.0 * ns + 24.0 * nc;
+    g->k_bytes[kcSkelDown] += (g->slope ? 25.0 : 17.0) * ns + 56.0 * nc;
+    g->k_bytes[kcSkelRank] += 24.0 * ns * rounds;
+}
+
 int run_basin_pass(fl_graph* g, int* changed) {
     FL_TRY(clear_flags(g));
     g->stamp = g->stamp == 0x7ffffff0 ? 1 : g->stamp + 1;
@@ -608,6 +630,7 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.hgt = g->d_hgt;
     a.order = g->d_order;
     a.roff = g->d_roff;
+    a.rtime = g->d_rtime;
     a.max_rounds = g->max_rounds;
     a.kahn_min_width = g->kahn_min_width;
     a.meta = g->d_meta;
@@ -651,6 +674,7 @@ int run_basin_pass(fl_graph* g, int* changed) {
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
     FL_TRY(device_error(h));
+    account_skeleton(g);
     *changed = h[kChanged];
     return FL_OK;
 }
@@ -975,9 +999,33 @@ uint32_t fl_num_kernel_classes(void) { return kcCount; }
 
 int fl_graph_basin_stats(const fl_graph* g, uint64_t* out, uint32_t cap) {
     if (!g) return FL_ERR_MODEL_NOT_SET;
-    const uint32_t idx[] = {kMetaRStop, kMetaLeaves, kMetaNs, kMetaChains, kMetaMaxChain,
-                            kMetaSlow, kMetaSpinUp, kMetaSpinDown};
-    for (uint32_t i = 0; i < cap && i < sizeof idx / sizeof idx[0]; ++i) out[i] = g->last_meta[idx[i]];
+    const uint32_t* m = g->last_meta;
+    auto u64 = [&](int slot) { return (uint64_t)m[slot] | ((uint64_t)m[slot + 1] << 32); };
+    const uint64_t up = u64(kMetaUpSlow), down = u64(kMetaDownSlow);
+    const uint64_t vals[] = {m[kMetaRStop], m[kMetaLeaves], m[kMetaNs], m[kMetaChains],
+                             m[kMetaMaxChain], m[kMetaSlow], m[kMetaSpinUp], m[kMetaSpinDown],
+                             (up >> kStatDurShift) << 6, ((up >> kStatCycShift) & kStat22) << 7,
+                             up & kStat20,
+                             (down >> kStatDurShift) << 6, ((down >> kStatCycShift) & kStat22) << 7,
+                             down & kStat20};
+    for (uint32_t i = 0; i < cap && i < sizeof vals / sizeof vals[0]; ++i) out[i] = vals[i];
+    return FL_OK;
+}
+
+int fl_graph_round_trace(fl_graph* g, uint32_t cap, uint32_t* rounds, uint32_t* offsets,
+                         uint64_t* up_ns, uint64_t* down_ns) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    if (!rounds) return FL_ERR_INVALID_ARGUMENT;
+    FL_CU(cudaSetDevice(g->device));
+    const uint32_t r = g->last_meta[kMetaRStop];
+    *rounds = r;
+    const uint32_t k = std::min<uint32_t>(cap, r + 1);
+    if (k == 0 || !g->d_rtime) return FL_OK;
+    if (offsets) FL_CU(cudaMemcpy(offsets, g->d_roff, k * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (up_ns) FL_CU(cudaMemcpy(up_ns, g->d_rtime, k * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    if (down_ns)
+        FL_CU(cudaMemcpy(down_ns, g->d_rtime + g->max_rounds + 1, k * sizeof(uint64_t),
+                         cudaMemcpyDeviceToHost));
     return FL_OK;
 }
 

@@ -113,8 +113,19 @@ int fl_graph_kernel_stats(const fl_graph* g, uint32_t cls, const char** name, ui
 
 /* Shape of the last basin pass (up to `cap` values): Kahn rounds run, leaves,
  * skeleton sites, skeleton chains, longest chain, skeleton sites needing the full
- * pull while walking, bottom-up and top-down hand-off wait iterations. */
+ * pull while walking, bottom-up and top-down hand-off wait iterations; then the
+ * slowest bottom-up chain's walk time (ns), SM cycles spent in its full pulls and
+ * their number; the slowest top-down chain's walk time (ns), SM cycles waiting for
+ * its parent and its length.  Durations are kept to 64 ns, cycles to 128. */
 int fl_graph_basin_stats(const fl_graph* g, uint64_t* out, uint32_t cap);
+
+/* Round structure of the last basin pass (instrumentation; no fastlem counterpart).
+ * *rounds = Kahn rounds run (r); for k <= min(cap - 1, r): offsets[k] = first order
+ * slot of Kahn round k, up_ns[k] = device clock (ns) when bottom-up round k started
+ * (up_ns[r] = end), down_ns[k] = when the k-th top-down round started (highest Kahn
+ * round first; down_ns[r] = end).  Any output pointer may be NULL. */
+int fl_graph_round_trace(fl_graph* g, uint32_t cap, uint32_t* rounds, uint32_t* offsets,
+                         uint64_t* up_ns, uint64_t* down_ns);
 
 /* ---- parity probes: one solver stage on host arrays (tests only) ---------------- */
 
