@@ -41,15 +41,20 @@
 namespace fl {
 namespace {
 
-__device__ __forceinline__ void prefetch_l1(const void* p) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
-// per-slot flags of the skeleton layout
-constexpr uint8_t kLeafSlot = 1;   // chain leaf: pre holds the complete area
-constexpr uint8_t kSlow = 4;       // confluence or > kMaxPost additions: full pull at walk time
-constexpr int kPostShift = 3;      // bits 3-4: additions after the chain predecessor (0..3)
+// per-slot flags of the skeleton layout (SlotInfo::flags)
+constexpr uint32_t kLeafSlot = 1;  // chain leaf: pre holds the complete area
+constexpr uint32_t kTok = 2;       // donor list in tokval (a confluence with another chain's
+                                   // bottom, or more than kMaxPost additions after the
+                                   // predecessor)
+constexpr uint32_t kSlow = 4;      // donor list too long: full pull at walk time
+constexpr int kPostShift = 3;      // bits 3-4: additions after the chain predecessor
 constexpr int kMaxPost = 3;
+constexpr int kTokCntShift = 8;    // bits 8-11: donor-list length (cell area first)
+constexpr int kHeavyShift = 12;    // bits 12-15: the predecessor's index in the list
+constexpr int kMaxTok = 15;
+// A chain bottom's area not pushed yet (a signalling NaN: never an arithmetic result,
+// and pushed NaNs are quieted).
+constexpr uint64_t kPendingBits = 0x7ff4000000000000ull;
 
 // Rows up to this many slots are gathered with all loads in flight at once; longer
 // rows (rare: hull sites) take the plain loop.
@@ -318,7 +323,7 @@ __global__ void k_s_scan(const uint32_t* __restrict__ clen, uint32_t* __restrict
 __global__ void k_s_layout(const uint32_t* __restrict__ slist, Ranks rk,
                            const uint32_t* __restrict__ cid, const uint32_t* __restrict__ coff,
                            uint32_t* __restrict__ layout, uint32_t* __restrict__ slot_chain,
-                           const uint32_t* meta, int* flags) {
+                           uint32_t* __restrict__ kslot, const uint32_t* meta, int* flags) {
     if (flags[kError]) return;
     uint32_t ns = meta[kMetaNs];
     const uint32_t* ptr = rk.P(meta);
@@ -329,6 +334,7 @@ __global__ void k_s_layout(const uint32_t* __restrict__ slist, Ranks rk,
         if (q < ns) {
             layout[q] = slist[k];
             slot_chain[q] = c;
+            kslot[k] = q;
         } else {
             set_error(flags, kErrForest);
         }
@@ -345,9 +351,9 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
                             const uint32_t* __restrict__ layout,
                             const uint32_t* __restrict__ slot_chain,
                             const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
-                            const uint32_t* __restrict__ cbot, double* __restrict__ pre,
-                            double* __restrict__ post, double* __restrict__ post1,
-                            double* __restrict__ post2, uint8_t* __restrict__ sflag,
+                            const uint32_t* __restrict__ cbot, SlotRec* __restrict__ rec,
+                            SlotInfo* __restrict__ info, double* __restrict__ tokval,
+                            uint32_t tok_cap, uint64_t* __restrict__ push_to,
                             int* __restrict__ td_need, int stamp, uint32_t* meta,
                             int* flags) {
     if (flags[kError]) return;
@@ -364,38 +370,74 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
         uint32_t heavy = q < last ? layout[q + 1] : kNone;
         double a = area[v];
         double ps[kMaxPost] = {0.0, 0.0, 0.0};
-        int np = 0;
-        uint8_t f = (q == last) ? kLeafSlot : 0;
-        bool seen_heavy = false;
-        // reverse row order: additions before the predecessor fold into pre, the ones
-        // after it are replayed by the walk
-        for (uint32_t s = row[v + 1]; s-- > row[v];) {
+        int np = 0, ndon = 0;
+        uint32_t f = (q == last) ? kLeafSlot : 0;
+        bool seen_heavy = false, list = false;
+        // reverse row order: additions before the predecessor fold into pre, up to
+        // kMaxPost after it are replayed by the walk; anything else keeps the whole
+        // donor list
+        const uint32_t s0 = row[v], s1 = row[v + 1];
+        for (uint32_t s = s1; s-- > s0;) {
             uint32_t d = col[s];
             if (d == v || next[d] != v) continue;
+            ++ndon;
             if (d == heavy) {
                 seen_heavy = true;
                 continue;
             }
-            if (hgt[d] == kNone) {          // another chain's bottom: resolved at walk time
-                f |= kSlow;
-                break;
+            if (hgt[d] == kNone) {          // another chain's bottom: pushed at walk time
+                list = true;
+                continue;
             }
+            if (list) continue;
             double val = A[d];
             if (!seen_heavy) {
                 a = __dadd_rn(a, val);
             } else if (np < kMaxPost) {
-                ps[np++] = val;
+                if (np == 0) ps[0] = val;
+                else if (np == 1) ps[1] = val;
+                else ps[2] = val;
+                ++np;
             } else {
-                f |= kSlow;
-                break;
+                list = true;
             }
         }
-        pre[q] = a;
-        post[q] = ps[0];
-        post1[q] = ps[1];
-        post2[q] = ps[2];
-        sflag[q] = f | (uint8_t)(np << kPostShift);
-        warp_append(&meta[kMetaSlow], (f & kSlow) != 0);
+        uint32_t toff = 0;
+        if (list) {
+            const uint32_t nt = 1 + (uint32_t)ndon;
+            toff = kNone;
+            if (nt <= (uint32_t)kMaxTok) {
+                toff = atomicAdd(&meta[kMetaTok], nt);
+                if (toff + nt > tok_cap) toff = kNone;
+            }
+            if (toff == kNone) {
+                f |= kSlow;
+                toff = 0;
+            } else {
+                tokval[toff] = area[v];
+                uint32_t t = 1, hpos = 0;
+                for (uint32_t s = s1; s-- > s0;) {
+                    uint32_t d = col[s];
+                    if (d == v || next[d] != v) continue;
+                    double val = 0.0;
+                    if (d == heavy) {
+                        hpos = t;
+                    } else if (hgt[d] == kNone) {
+                        val = __longlong_as_double((long long)kPendingBits);
+                        push_to[d] = ((uint64_t)(uint32_t)stamp << 32) | (toff + t);
+                    } else {
+                        val = A[d];
+                    }
+                    tokval[toff + t] = val;
+                    ++t;
+                }
+                f |= kTok | (nt << kTokCntShift) | (hpos << kHeavyShift);
+            }
+            np = 0;
+        }
+        rec[q] = SlotRec{a, ps[0], ps[1], ps[2]};
+        info[q] = SlotInfo{f | ((uint32_t)np << kPostShift), toff};
+        warp_append(&meta[kMetaSlow], (f & (kTok | kSlow)) != 0);
     }
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         uint32_t b = cbot[c];
@@ -404,7 +446,6 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
     }
 }
 
-constexpr int kBatch = 8;
 constexpr unsigned kFull = 0xffffffffu;
 
 // Keeps the slowest chain's walk statistic in meta[slot] (two words).
@@ -472,21 +513,92 @@ __device__ double warp_slow_pull(uint32_t v, uint32_t heavy, double x,
     return acc;
 }
 
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const double* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(double* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// The full pull of a slot with a donor list, by the whole warp: lane t takes entry t
+// (waiting for a chain bottom's push), then the entries are added in order to the cell
+// area, x standing in for the chain predecessor.
+__device__ double warp_list_pull(const double* tokval, uint32_t toff, uint32_t nt, uint32_t hpos,
+                                 double x, int* flags, bool* ok, uint32_t* spin_total) {
+    const int lane = threadIdx.x & 31;
+    double v = 0.0;
+    bool fail = false;
+    if ((uint32_t)lane < nt) {
+        uint64_t b = ld_relaxed_u64(&tokval[toff + lane]);
+        uint32_t spins = 0;
+        while (b == kPendingBits) {
+            if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&flags[kError]))) {
+                set_error(flags, kErrWait);
+                fail = true;
+                break;
+            }
+            __nanosleep(32);
+            b = ld_relaxed_u64(&tokval[toff + lane]);
+        }
+        *spin_total += spins;
+        v = __longlong_as_double((long long)b);
+    }
+    if (__any_sync(kFull, fail)) {
+        *ok = false;
+        return 0.0;
+    }
+    double acc = __shfl_sync(kFull, v, 0);
+    for (uint32_t t = 1; t < nt; ++t) {
+        const double vt = __shfl_sync(kFull, v, t);
+        acc = __dadd_rn(acc, t == hpos ? x : vt);
+    }
+    return acc;
+}
+
 // One warp per chain, leaf to bottom.  Each round the lanes load 32 slots (lane l the
 // slot l places below the round's top, coalesced) and issue the next round's loads;
-// warp_fold then applies every slot's additions to the running area exactly (integer
-// scan between binade crossings and ties, f64 additions for those).  Chain leaves and
-// confluences are evaluated one at a time.  Results go to Al (layout order); the chain
-// bottom's area is also stored in A and published through bu_done.
-__global__ void __launch_bounds__(kWalkWarps * 32, 7) k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
-                              const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
-                              const double* __restrict__ area, double* A,
-                              const uint32_t* __restrict__ layout,
-                              const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
-                              const double* __restrict__ pre, const double* __restrict__ post,
-                              const double* __restrict__ post1, const double* __restrict__ post2,
-                              const uint8_t* __restrict__ sflag, double* __restrict__ Al,
-                              int* bu_done, int stamp, uint32_t* meta, int* flags) {
+// warp_fold then applies every slot's additions (pre, then post) to the running area
+// exactly.  Chain leaves and slots with a donor list are evaluated one at a time by
+// the warp.  Results go to Al (layout order); the chain bottom's area is also stored
+// in A and published through bu_done, and pushed into the donor list that waits for
+// it.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Rounds of slot data in flight ahead of the one being folded (per warp, in shared
+// memory: a lane only ever reads back what it copied itself).  A folded round takes
+// well under the L2 / HBM latency, so several rounds must be in flight.
+constexpr int kStages = 3;
+constexpr int kStagesDown = 4;
+// Consecutive slots per lane and round: one warp scan covers 32 * S slots.
+constexpr int kUpSlots = 2;
+constexpr int kDownSlots = 4;
+
+__global__ void __launch_bounds__(kWalkWarps * 32, 7)
+k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
+              const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
+              const double* __restrict__ area, double* A, const uint32_t* __restrict__ layout,
+              const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
+              const SlotRec* __restrict__ rec, const SlotInfo* __restrict__ info,
+              double* tokval, const uint64_t* __restrict__ push_to, double* __restrict__ Al,
+              int* bu_done, int stamp, uint32_t* meta, int* flags) {
+    constexpr int S = kUpSlots;
+    __shared__ SlotRec s_rec[kWalkWarps][kStages][32 * S];
+    __shared__ SlotInfo s_info[kWalkWarps][kStages][32 * S];
     const int lane = threadIdx.x & 31;
     const int wb = threadIdx.x >> 5;
     const uint32_t c = blockIdx.x * kWalkWarps + wb;
@@ -500,57 +612,90 @@ __global__ void __launch_bounds__(kWalkWarps * 32, 7) k_s_bottom_up(const uint32
     }
     const uint64_t t_start = global_ns();
     uint32_t slow_cycles = 0, slow_n = 0;
-    const int64_t lo = off;
-    int64_t top = (int64_t)off + len - 1;
-    double y[kFoldOps] = {0.0, 0.0, 0.0, 0.0};
-    uint8_t f = 0;
-    auto load = [&](int64_t t, double (&dst)[kFoldOps], uint8_t& fl_) {
-        int64_t q = t - lane;
-        if (q >= lo) {
-            dst[0] = pre[q];
-            dst[1] = post[q];
-            dst[2] = post1[q];
-            dst[3] = post2[q];
-            fl_ = sflag[q];
+    // round r, lane l, slot s is the slot (32 r + l) S + s places below the chain's leaf
+    const uint32_t per_round = 32 * S;
+    const uint32_t nrounds = (len + per_round - 1) / per_round;
+    const uint32_t top = off + len - 1;
+    auto issue = [&](uint32_t r) {                   // one commit group per round
+        if (r < nrounds) {
+#pragma unroll
+            for (int sl = 0; sl < S; ++sl) {
+                const uint32_t back = r * per_round + lane * S + sl;
+                if (back < len) {
+                    const uint32_t q = top - back;
+                    SlotRec* dst = &s_rec[wb][r % kStages][lane * S + sl];
+                    cp_async16(&dst->pre, &rec[q].pre);
+                    cp_async16(&dst->p1, &rec[q].p1);
+                    cp_async8(&s_info[wb][r % kStages][lane * S + sl], &info[q]);
+                }
+            }
         }
+        cp_async_commit();
     };
-    load(top, y, f);
+#pragma unroll
+    for (int r = 0; r < kStages - 1; ++r) issue(r);
     double x = 0.0;
     bool ok = true;
     uint32_t spins = 0;
-    for (; top >= lo; top -= 32) {
-        double ny[kFoldOps] = {0.0, 0.0, 0.0, 0.0};
-        uint8_t nf = 0;
-        load(top - 32, ny, nf);                       // next round in flight
-        const int64_t left = top - lo + 1;
-        const int cnt = left < 32 ? (int)left : 32;
-        const bool special = (f & (kLeafSlot | kSlow)) != 0;
-        const int nop = 1 + ((f >> kPostShift) & 3);
-        const int64_t t0 = top;
-        double mine = 0.0;
-        x = warp_fold(x, y, nop, special, cnt, mine, [&](int k, double xin) -> double {
-            const uint8_t fk = (uint8_t)__shfl_sync(kFull, (uint32_t)f, k);
-            const double pk = __shfl_sync(kFull, y[0], k);
-            if (fk & kLeafSlot) return pk;             // chain leaf: its own complete pull
-            if (!ok) return xin;
-            const long long c0 = clock64();
-            const double r = warp_slow_pull(layout[t0 - k], layout[t0 - k + 1], xin, row, col,
-                                            next, hgt, area, A, bu_done, stamp, flags, &ok, &spins);
-            slow_cycles += (uint32_t)(clock64() - c0);
-            ++slow_n;
-            return r;
-        });
-        if (!ok) return;
-        if (lane < cnt) Al[top - lane] = mine;
+    for (uint32_t r = 0; r < nrounds; ++r) {
+        __syncwarp();                                // stage r - 1 is no longer read
+        issue(r + kStages - 1);
+        cp_async_wait<kStages - 1>();                // this round's copies have landed
+        __syncwarp();                                // ... for every lane
+        const int st = r % kStages;
+        const uint32_t left = len - r * per_round;
+        const int cnt = left < per_round ? (int)((left + S - 1) / S) : 32;
+        const int nsl = (uint32_t)lane * S < left ? (int)min((uint32_t)S, left - lane * S) : 0;
+        uint32_t nopm = 0, specm = 0;
 #pragma unroll
-        for (int j = 0; j < kFoldOps; ++j) y[j] = ny[j];
-        f = nf;
+        for (int sl = 0; sl < S; ++sl) {
+            if (sl < nsl) {
+                const uint32_t fl = s_info[wb][st][lane * S + sl].flags;
+                nopm |= ((fl >> kPostShift) & 3u) << (2 * sl);
+                if (fl & (kLeafSlot | kTok | kSlow)) specm |= 1u << sl;
+            }
+        }
+        auto opnd = [&](int l, int sl, int j) -> double {
+            return reinterpret_cast<const double*>(&s_rec[wb][st][l * S + sl])[j];
+        };
+        x = warp_fold_slots<S, 4>(
+            x, cnt, nsl, nopm, specm, [&](int sl, int j) { return opnd(lane, sl, j); },
+            [&](int l, int sl, int j) { return opnd(l, sl, j); },
+            [&](int l, int sl, double xin) -> double {
+                const SlotInfo si = s_info[wb][st][l * S + sl];
+                const uint32_t q = top - (r * per_round + l * S + sl);
+                if (!ok) return xin;
+                const long long c0 = clock64();
+                double res;
+                if (si.flags & kTok) {
+                    res = warp_list_pull(tokval, si.tokoff, (si.flags >> kTokCntShift) & 15u,
+                                         (si.flags >> kHeavyShift) & 15u, xin, flags, &ok, &spins);
+                } else if (si.flags & kSlow) {
+                    res = warp_slow_pull(layout[q], (si.flags & kLeafSlot) ? kNone : layout[q + 1],
+                                         xin, row, col, next, hgt, area, A, bu_done, stamp, flags,
+                                         &ok, &spins);
+                } else {
+                    return opnd(l, sl, 0);             // chain leaf: its own complete pull
+                }
+                slow_cycles += (uint32_t)(clock64() - c0);
+                ++slow_n;
+                return res;
+            },
+            [&](int sl, double v) { Al[top - (r * per_round + lane * S + sl)] = v; });
+        if (!ok) break;
     }
+    cp_async_wait<0>();                              // nothing in flight at exit
+    if (!ok) return;
     if (lane == 0) {
         uint32_t bottom = layout[off];
         A[bottom] = x;
-        __threadfence();
-        st_release(&bu_done[bottom], stamp);
+        st_release(&bu_done[bottom], stamp);          // orders the store above
+        const uint64_t pt = push_to[bottom];
+        if ((uint32_t)(pt >> 32) == (uint32_t)stamp) {
+            uint64_t xb = (uint64_t)__double_as_longlong(x);
+            if (isnan(x)) xb = 0x7ff8000000000000ull;   // never the pending marker
+            st_relaxed_u64(&tokval[(uint32_t)pt], xb);
+        }
     }
     spins = __reduce_add_sync(kFull, spins);
     if (lane == 0 && spins) atomicAdd(&meta[kMetaSpinUp], spins);
@@ -566,17 +711,19 @@ __global__ void k_s_scatter(const uint32_t* __restrict__ layout, const double* _
         dst[layout[q]] = src[q];
 }
 
-// Top-down operands in layout order: w, and whether another chain waits for the site.
+// Top-down operands in layout order: w, and whether another chain waits for the site;
+// every layout-order response time starts as the pending marker.
 __global__ void k_s_gather_down(const uint32_t* __restrict__ layout, const double* __restrict__ w,
                                 const int* __restrict__ td_need, int stamp,
                                 double* __restrict__ wl, uint8_t* __restrict__ needl,
-                                const uint32_t* meta, const int* flags) {
+                                double* __restrict__ tl, const uint32_t* meta, const int* flags) {
     if (flags[kError]) return;
     uint32_t ns = meta[kMetaNs];
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x) {
         uint32_t v = layout[q];
         wl[q] = w[v];
         needl[q] = td_need[v] == stamp ? 1 : 0;
+        tl[q] = __longlong_as_double((long long)kPendingBits);
     }
 }
 
@@ -637,146 +784,222 @@ __device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t
     return tv;
 }
 
+// Per chain, before the top-down walk (one block): the layout slot of the site it
+// hangs from (kNone for a chain that starts at a root), and its basin outlet with the
+// outlet's response time and elevation, inherited from the chain tree's root chain by
+// pointer jumping.  Root sites are settled here (t = 0 + (0 + w), elevation with the
+// outlet's own update), and their response time / elevation stored in the layout
+// arrays and published for the slope-limited walk.
+__global__ void k_s_chain_roots(TopDown td, const uint32_t* __restrict__ layout,
+                                const uint32_t* __restrict__ coff,
+                                const uint32_t* __restrict__ sid,
+                                const uint32_t* __restrict__ kslot,
+                                const uint32_t* __restrict__ slot_chain, uint32_t* cpar,
+                                uint32_t* __restrict__ cqp, uint32_t* __restrict__ cbas,
+                                double* __restrict__ cto, double* __restrict__ ceo,
+                                double* __restrict__ tl, double* __restrict__ el, int* td_done,
+                                int stamp, const uint32_t* meta) {
+    if (td.flags[kError]) return;
+    const uint32_t nc = meta[kMetaChains];
+    bool changed = false;
+    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
+        const uint32_t off = coff[c];
+        const uint32_t v = layout[off];
+        const uint32_t p = td.next[v];
+        if (p == v) {
+            double e;
+            const double tv = settle(td, v, v, 0.0, kNone, 0.0, 0.0, 0.0, &e, &changed);
+            tl[off] = tv;
+            el[off] = e;
+            cpar[c] = c;
+            cqp[c] = kNone;
+            cbas[c] = td.outlet[v] ? v : kNone;
+            cto[c] = tv;
+            ceo[c] = e;
+            td_done[v] = stamp;
+        } else {
+            const uint32_t qp = kslot[sid[p]];
+            cqp[c] = qp;
+            cpar[c] = slot_chain[qp];
+        }
+    }
+    __syncthreads();
+    // root chain of every chain; values only ever move to ancestors, so the in-place
+    // update needs no second buffer
+    bool moved = true;
+    for (int round = 0; round < 40 && moved; ++round) {
+        bool any = false;
+        for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
+            const uint32_t r = cpar[c];
+            const uint32_t rr = cpar[r];
+            if (rr != r) {
+                cpar[c] = rr;
+                any = true;
+            }
+        }
+        moved = __syncthreads_or(any) != 0;
+    }
+    if (moved) {
+        if (threadIdx.x == 0) set_error(td.flags, kErrForest);
+        return;
+    }
+    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
+        const uint32_t r = cpar[c];
+        if (r != c) {
+            cbas[c] = cbas[r];
+            cto[c] = cto[r];
+            ceo[c] = ceo[r];
+        }
+    }
+    block_flag(td.flags, kChanged, changed);
+}
+
 // One warp per chain, bottom to leaf: t_v = 0 + (t_parent + w_v) (below a root t is
-// never -0.0, so that is t_parent + w_v).  Rounds of 32 slots as in the bottom-up
-// walk.  Without slope limits only t is carried (tl, layout order; elevations follow
-// in k_s_finish); with them lane 0 carries the elevation and its clamp too.  The
-// chain's basin outlet and its t / elevation are stored per chain.  Sites another
-// chain waits for are written to t / elev / bas directly and published.
-__global__ void k_s_top_down(TopDown td, const uint32_t* __restrict__ layout,
-                             const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
-                             const double* __restrict__ wl, const uint8_t* __restrict__ needl,
-                             double* __restrict__ tl, double* __restrict__ el,
-                             uint32_t* __restrict__ cbas, double* __restrict__ cto,
-                             double* __restrict__ ceo, bool slope, int* td_done, int stamp,
-                             uint32_t* meta) {
+// never -0.0, so that is t_parent + w_v), in rounds of 32 slots folded exactly.
+// Without slope limits only t is needed (tl, layout order; elevations follow in
+// k_s_finish): a chain waits until its parent slot's tl is no longer the pending
+// marker, and every tl it writes is itself the publication for the chains below.
+__global__ void __launch_bounds__(kWalkWarps * 32, 8)
+k_s_top_down(const int* flags, const uint32_t* __restrict__ coff,
+             const uint32_t* __restrict__ clen, const uint32_t* __restrict__ cqp,
+             const double* __restrict__ wl, double* tl, uint32_t* meta) {
     const int lane = threadIdx.x & 31;
     const int wb = threadIdx.x >> 5;
     const uint32_t c = blockIdx.x * kWalkWarps + wb;
     // warp-uniform exits only: the warp shuffles with the full mask below
-    if (c >= meta[kMetaChains] || __any_sync(kFull, ld_acquire(&td.flags[kError]) != 0)) return;
+    if (c >= meta[kMetaChains] || __any_sync(kFull, ld_acquire(&flags[kError]) != 0)) return;
     const uint32_t off = coff[c], len = clen[c];
     if (off + len > meta[kMetaNs] || len == 0) {
-        if (lane == 0) set_error(td.flags, kErrForest);
+        if (lane == 0) set_error(const_cast<int*>(flags), kErrForest);
         return;
     }
     const uint32_t end = off + len;
-    // chain start (lane 0), then broadcast
-    uint32_t v = layout[off];
-    uint32_t p = td.next[v];
-    double tp = 0.0, ep = 0.0, to = 0.0, eo = 0.0;
-    uint32_t o = kNone;
+    const uint32_t qp = cqp[c];
     uint32_t q = off;
-    bool changed = false;
+    uint64_t tb = 0;
     bool failed = false;
-    if (lane == 0) {
-        if (p == v) {                     // the chain starts at a root
-            double e;
-            tp = settle(td, v, p, 0.0, kNone, 0.0, 0.0, 0.0, &e, &changed);
-            ep = e;
-            o = td.outlet[v] ? v : kNone;
-            to = tp;
-            eo = e;
-            tl[q] = tp;
-            if (slope) el[q] = e;
-            if (needl[q]) {
-                __threadfence();
-                st_release(&td_done[v], stamp);
+    if (qp == kNone) {                   // the root was settled before the walk
+        tb = (uint64_t)__double_as_longlong(tl[off]);
+        q = off + 1;
+    } else if (lane == 0) {
+        uint32_t spins = 0;
+        const uint64_t t0 = global_ns();
+        const long long c0 = clock64();
+        tb = ld_relaxed_u64(&tl[qp]);
+        while (tb == kPendingBits) {
+            if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&flags[kError]))) {
+                set_error(const_cast<int*>(flags), kErrWait);
+                failed = true;
+                break;
             }
-        } else {
-            uint32_t spins = 0;
-            const uint64_t t0 = global_ns();
-            const long long c0 = clock64();
-            while (ld_acquire(&td_done[p]) != stamp) {
-                if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
-                    set_error(td.flags, kErrWait);
-                    failed = true;
-                    break;
-                }
-                __nanosleep(32);
-            }
-            // the chain that waited longest for its parent
-            record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
-            if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
-            if (!failed) {
-                tp = __ldcg(&td.t[p]);
-                ep = __ldcg(&td.elev[p]);
-                o = __ldcg(&td.bas[p]);
-                if (o != kNone) {
-                    to = __ldcg(&td.t[o]);
-                    eo = __ldcg(&td.elev[o]);
-                }
-            }
+            __nanosleep(32);
+            tb = ld_relaxed_u64(&tl[qp]);
         }
-        cbas[c] = o;
-        cto[c] = to;
-        ceo[c] = eo;
+        // the chain that waited longest for its parent
+        record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
+        if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
     }
     if (__shfl_sync(kFull, failed, 0)) return;
-    if (p == v) q = off + 1;
-    tp = __shfl_sync(kFull, tp, 0);
-    ep = __shfl_sync(kFull, ep, 0);
-    o = __shfl_sync(kFull, o, 0);
-    to = __shfl_sync(kFull, to, 0);
-    eo = __shfl_sync(kFull, eo, 0);
-    if (slope) {
-        // lane 0 carries the elevation clamp site by site
-        if (lane == 0) {
-            for (; q < end; ++q) {
-                v = layout[q];
-                double e;
-                tp = settle(td, v, p, tp, o, to, eo, ep, &e, &changed);
-                tl[q] = tp;
-                el[q] = e;
-                ep = e;
-                p = v;
-                if (needl[q]) {
-                    __threadfence();
-                    st_release(&td_done[v], stamp);
-                }
+    double tp = __longlong_as_double((long long)__shfl_sync(kFull, (unsigned long long)tb, 0));
+    constexpr int S = kDownSlots;
+    constexpr uint32_t per_round = 32 * S;
+    __shared__ double s_w[kWalkWarps][kStagesDown][32 * S];
+    const uint32_t nrounds = (end - q + per_round - 1) / per_round;
+    auto issue = [&](uint32_t r) {                   // one commit group per round
+        if (r < nrounds) {
+#pragma unroll
+            for (int sl = 0; sl < S; ++sl) {
+                const uint32_t qq = q + r * per_round + lane * S + sl;
+                if (qq < end) cp_async8(&s_w[wb][r % kStagesDown][lane * S + sl], &wl[qq]);
             }
-            if (changed) td.flags[kChanged] = 1;
         }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int r = 0; r < kStagesDown - 1; ++r) issue(r);
+    for (uint32_t r = 0; r < nrounds; ++r) {
+        __syncwarp();                                // stage r - 1 is no longer read
+        issue(r + kStagesDown - 1);
+        cp_async_wait<kStagesDown - 1>();
+        __syncwarp();
+        const int st = r % kStagesDown;
+        const uint32_t q0 = q + r * per_round;
+        const uint32_t left = end - q0;
+        const int cnt = left < per_round ? (int)((left + S - 1) / S) : 32;
+        const int nsl = (uint32_t)lane * S < left ? (int)min((uint32_t)S, left - lane * S) : 0;
+        tp = warp_fold_slots<S, 1>(
+            tp, cnt, nsl, 0u, 0u, [&](int sl, int) { return s_w[wb][st][lane * S + sl]; },
+            [&](int l, int sl, int) { return s_w[wb][st][l * S + sl]; },
+            [](int, int, double xin) -> double { return xin; },
+            [&](int sl, double v) {
+                st_relaxed_u64(&tl[q0 + lane * S + sl], (uint64_t)__double_as_longlong(v));
+            });
+    }
+    cp_async_wait<0>();
+}
+
+// With slope limits the elevation clamp e_v <= e_parent + tan * len chains through
+// the elevations too: lane 0 walks the chain site by site with settle().  A chain
+// starts once its parent site is published (t / elevation / basin written, then
+// td_done released); sites another chain hangs from are published as they are
+// passed.  Root chains start from the values the pre-pass settled.
+__global__ void k_s_top_down_slope(TopDown td, const uint32_t* __restrict__ layout,
+                                   const uint32_t* __restrict__ coff,
+                                   const uint32_t* __restrict__ clen,
+                                   const uint32_t* __restrict__ cqp,
+                                   const uint8_t* __restrict__ needl, double* __restrict__ tl,
+                                   double* __restrict__ el, const uint32_t* __restrict__ cbas,
+                                   const double* __restrict__ cto, const double* __restrict__ ceo,
+                                   int* td_done, int stamp, uint32_t* meta) {
+    const int lane = threadIdx.x & 31;
+    const int wb = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * kWalkWarps + wb;
+    if (lane != 0) return;
+    if (c >= meta[kMetaChains] || ld_acquire(&td.flags[kError]) != 0) return;
+    const uint32_t off = coff[c], len = clen[c];
+    if (off + len > meta[kMetaNs] || len == 0) {
+        set_error(td.flags, kErrForest);
         return;
     }
-    double rw = 0.0;
-    uint8_t rn = 0;
-    if (q + lane < end) {
-        rw = wl[q + lane];
-        rn = needl[q + lane];
-    }
-    for (; q < end; q += 32) {
-        const double wv = rw;
-        const uint8_t need = rn;
-        if (q + 32 + lane < end) {                 // next round in flight
-            rw = wl[q + 32 + lane];
-            rn = needl[q + 32 + lane];
-        }
-        const int cnt = (end - q) < 32u ? (int)(end - q) : 32;
-        double mine = 0.0;
-        const double yv[kFoldOps] = {wv, 0.0, 0.0, 0.0};
-        tp = warp_fold(tp, yv, 1, false, cnt, mine,
-                       [](int, double xin) -> double { return xin; });
-        if (lane < cnt) {
-            tl[q + lane] = mine;
-            if (need) {                             // another chain hangs here: publish
-                uint32_t u = layout[q + lane];
-                double old_e = __ldcg(&td.elev[u]);
-                double e = old_e;
-                if (o != kNone) {
-                    double dt = __dsub_rn(mine, to);
-                    e = __dadd_rn(eo, __dmul_rn(td.uu[u], dt > 0.0 ? dt : 0.0));
-                    if (e != old_e) changed = true;
-                }
-                td.t[u] = mine;
-                td.elev[u] = e;
-                td.bas[u] = o;
-                __threadfence();
-                st_release(&td_done[u], stamp);
+    const uint32_t end = off + len;
+    uint32_t q = off;
+    uint32_t p = td.next[layout[off]];
+    double tp, ep;
+    const uint32_t o = cbas[c];
+    const double to = cto[c], eo = ceo[c];
+    if (cqp[c] == kNone) {
+        tp = tl[off];
+        ep = el[off];
+        p = layout[off];
+        q = off + 1;
+    } else {
+        uint32_t spins = 0;
+        const uint64_t t0 = global_ns();
+        const long long c0 = clock64();
+        while (ld_acquire(&td_done[p]) != stamp) {
+            if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
+                set_error(td.flags, kErrWait);
+                return;
             }
+            __nanosleep(32);
         }
+        record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
+        if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
+        tp = __ldcg(&td.t[p]);
+        ep = __ldcg(&td.elev[p]);
     }
-    if (__any_sync(kFull, changed) && lane == 0) td.flags[kChanged] = 1;
+    bool changed = false;
+    for (; q < end; ++q) {
+        const uint32_t v = layout[q];
+        double e;
+        tp = settle(td, v, p, tp, o, to, eo, ep, &e, &changed);
+        tl[q] = tp;
+        el[q] = e;
+        ep = e;
+        p = v;
+        if (needl[q]) st_release(&td_done[v], stamp);   // t / elev / bas of v written above
+    }
+    if (changed) td.flags[kChanged] = 1;
 }
 
 // Skeleton response times and elevations back to site order.
@@ -871,14 +1094,19 @@ constexpr unsigned kRoundBlock = 1024;
 // Probe: x_k after each operand of one chain (one operand per slot), by warp_fold.
 __global__ void k_fold_probe(const double* __restrict__ y, uint32_t n, double x0,
                              double* __restrict__ out) {
+    constexpr int S = kDownSlots;
+    constexpr uint32_t per_round = 32 * S;
     const int lane = threadIdx.x & 31;
     double x = x0;
-    for (uint32_t base = 0; base < n; base += 32) {
-        const int cnt = (n - base) < 32u ? (int)(n - base) : 32;
-        const double yv[kFoldOps] = {base + lane < n ? y[base + lane] : 0.0, 0.0, 0.0, 0.0};
-        double mine = 0.0;
-        x = warp_fold(x, yv, 1, false, cnt, mine, [](int, double xin) -> double { return xin; });
-        if (lane < cnt) out[base + lane] = mine;
+    for (uint32_t base = 0; base < n; base += per_round) {
+        const uint32_t left = n - base;
+        const int cnt = left < per_round ? (int)((left + S - 1) / S) : 32;
+        const int nsl = (uint32_t)lane * S < left ? (int)min((uint32_t)S, left - lane * S) : 0;
+        x = warp_fold_slots<S, 1>(
+            x, cnt, nsl, 0u, 0u, [&](int sl, int) { return y[base + lane * S + sl]; },
+            [&](int l, int sl, int) { return y[base + l * S + sl]; },
+            [](int, int, double xin) -> double { return xin; },
+            [&](int sl, double v) { out[base + lane * S + sl] = v; });
     }
 }
 
@@ -893,6 +1121,9 @@ uint32_t walk_capacity() {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&up, k_s_bottom_up, kWalkWarps * 32, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&down, k_s_top_down, kWalkWarps * 32, 0);
+    int down_slope = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&down_slope, k_s_top_down_slope, kWalkWarps * 32, 0);
+    down = std::min(down, down_slope);
     int per = std::max(1, std::min(up, down));
     return (uint32_t)(sms * per * kWalkWarps);
 }
@@ -948,21 +1179,23 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     k_s_lengths<<<gs, kThreads, 0, st>>>(a.order, a.sid, rk, a.cid, a.clen, a.kahn_min_width, a.meta,
                                          a.flags);
     k_s_scan<<<1, 1024, 0, st>>>(a.clen, a.coff, a.meta, a.flags);
-    k_s_layout<<<gs, kThreads, 0, st>>>(a.slist, rk, a.cid, a.coff, a.layout, a.slot_chain, a.meta,
+    k_s_layout<<<gs, kThreads, 0, st>>>(a.slist, rk, a.cid, a.coff, a.layout, a.slot_chain, a.kslot,
+                                        a.meta,
                                         a.flags);
     k_s_prepare<<<gs, kThreads, 0, st>>>(n, a.row, a.col, a.next, a.hgt, a.area, a.A, a.layout,
-                                         a.slot_chain, a.coff, a.clen, a.cbot, a.pre, a.post,
-                                         a.post1, a.post2, a.sflag, a.td_need, a.stamp, a.meta,
-                                         a.flags);
+                                         a.slot_chain, a.coff, a.clen, a.cbot, a.rec, a.info,
+                                         a.tokval, a.tok_cap, a.push_to,
+                                         a.td_need, a.stamp, a.meta, a.flags);
     hk.end(hk.ctx, kcBasinBuild, 0.0);
 
     // chain walk bottom-up; results in layout order (in place over `pre`)
     hk.begin(hk.ctx);
     e = coop_launch(k_s_bottom_up, g_chain, kWalkWarps * 32, st, a.row, a.col, a.next,
                     (const uint32_t*)a.hgt, a.area, a.A, (const uint32_t*)a.layout,
-                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const double*)a.pre,
-                    (const double*)a.post, (const double*)a.post1, (const double*)a.post2,
-                    (const uint8_t*)a.sflag, a.pre, a.bu_done, a.stamp, a.meta, a.flags);
+                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const SlotRec*)a.rec,
+                    (const SlotInfo*)a.info, a.tokval, (const uint64_t*)a.push_to, a.pre,
+                    a.bu_done, a.stamp, a.meta,
+                    a.flags);
     hk.end(hk.ctx, kcSkelUp, 0.0);
     if (e != cudaSuccess) return e;
 
@@ -976,15 +1209,28 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     hk.end(hk.ctx, kcW, 32.0 * n);
 
     hk.begin(hk.ctx);
-    k_s_gather_down<<<gs, kThreads, 0, st>>>(a.layout, a.w, a.td_need, a.stamp, a.post, a.sflag,
-                                             a.meta, a.flags);
+    k_s_gather_down<<<gs, kThreads, 0, st>>>(a.layout, a.w, a.td_need, a.stamp, a.post, a.needl,
+                                             a.pre, a.meta, a.flags);
     hk.end(hk.ctx, kcBasinBuild, 0.0);
 
     hk.begin(hk.ctx);
-    e = coop_launch(k_s_top_down, g_chain, kWalkWarps * 32, st, td, (const uint32_t*)a.layout,
-                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const double*)a.post,
-                    (const uint8_t*)a.sflag, a.pre, a.el, a.cbas, a.cto, a.ceo, a.slope,
-                    a.td_done, a.stamp, a.meta);
+    k_s_chain_roots<<<1, kRoundBlock, 0, st>>>(td, (const uint32_t*)a.layout,
+                                               (const uint32_t*)a.coff, (const uint32_t*)a.sid,
+                                               (const uint32_t*)a.kslot,
+                                               (const uint32_t*)a.slot_chain, a.cpar, a.cqp,
+                                               a.cbas, a.cto, a.ceo, a.pre, a.el, a.td_done,
+                                               a.stamp, (const uint32_t*)a.meta);
+    if (a.slope) {
+        e = coop_launch(k_s_top_down_slope, g_chain, kWalkWarps * 32, st, td,
+                        (const uint32_t*)a.layout, (const uint32_t*)a.coff,
+                        (const uint32_t*)a.clen, (const uint32_t*)a.cqp, (const uint8_t*)a.needl,
+                        a.pre, a.el, (const uint32_t*)a.cbas, (const double*)a.cto,
+                        (const double*)a.ceo, a.td_done, a.stamp, a.meta);
+    } else {
+        e = coop_launch(k_s_top_down, g_chain, kWalkWarps * 32, st, (const int*)a.flags,
+                        (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const uint32_t*)a.cqp,
+                        (const double*)a.post, a.pre, a.meta);
+    }
     hk.end(hk.ctx, kcSkelDown, 0.0);
     if (e != cudaSuccess) return e;
 

@@ -47,7 +47,7 @@ enum Meta {
     kMetaSpinUp,       // wait iterations of the bottom-up chain hand-offs
     kMetaSpinDown,     // wait iterations of the top-down chain hand-offs
     kMetaMaxChain,     // longest skeleton chain
-    kMetaPad,
+    kMetaTok,          // used entries of the donor-list buffer
     kMetaUpSlow,       // (2 words, u64) slowest bottom-up chain, packed by pack_chain_stat
     kMetaUpSlowHi,
     kMetaDownSlow,     // (2 words, u64) slowest top-down chain, packed by pack_chain_stat
@@ -62,6 +62,19 @@ constexpr int kStatDurShift = 42;
 constexpr int kStatCycShift = 20;
 constexpr uint64_t kStat22 = (1ull << 22) - 1;
 constexpr uint64_t kStat20 = (1ull << 20) - 1;
+
+// Per skeleton layout slot, what the bottom-up walk adds to the chain's running area:
+// pre (the cell area plus the donors before the chain predecessor, in the reference's
+// order) and up to three donor areas after the predecessor.
+struct __align__(32) SlotRec {
+    double pre, p0, p1, p2;
+};
+// Per skeleton layout slot: kind bits, addition count, donor-list length and the
+// predecessor's position in it (see basin.cu), and the donor list's offset.
+struct __align__(8) SlotInfo {
+    uint32_t flags;
+    uint32_t tokoff;
+};
 
 struct BasinArgs {
     uint32_t n;
@@ -103,16 +116,22 @@ struct BasinArgs {
     uint32_t* coff;
     uint32_t* layout;
     uint32_t* slot_chain;   // layout slot -> chain
+    uint32_t* kslot;        // skeleton index -> layout slot
+    uint32_t* cpar;         // per chain: root chain of its chain tree (scratch)
+    uint32_t* cqp;          // per chain: layout slot of the site it hangs from, or kNone
     double* el;             // skeleton elevations in layout order (slope limits only)
     uint32_t* cbas;         // per chain: basin outlet, its response time and elevation
     double* cto;
     double* ceo;
     bool slope;             // some site has a maximum slope
-    double* pre;
-    double* post;
-    double* post1;
-    double* post2;
-    uint8_t* sflag;
+    SlotRec* rec;
+    SlotInfo* info;
+    double* pre;            // layout-order areas (bottom-up), response times (top-down)
+    double* post;           // layout-order w (top-down)
+    uint8_t* needl;         // per layout slot: another chain starts below this site
+    double* tokval;         // donor lists: final donor areas, chain bottoms pushed at walk time
+    uint32_t tok_cap;
+    uint64_t* push_to;      // per site: (stamp << 32) | tokval index its chain bottom fills
     int* bu_done;
     int* td_need;
     int* td_done;

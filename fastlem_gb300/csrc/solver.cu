@@ -269,10 +269,15 @@ struct fl_graph {
              *d_sptr0 = nullptr, *d_sdist0 = nullptr, *d_sptr1 = nullptr, *d_sdist1 = nullptr,
              *d_cid = nullptr, *d_cbot = nullptr, *d_clen = nullptr, *d_coff = nullptr,
              *d_layout = nullptr, *d_slot_chain = nullptr, *d_cbas = nullptr;
-    double *d_pre = nullptr, *d_post = nullptr, *d_post1 = nullptr, *d_post2 = nullptr,
+    double *d_pre = nullptr, *d_post = nullptr, *d_tokval = nullptr,
            *d_el = nullptr, *d_cto = nullptr, *d_ceo = nullptr;
     bool slope = false;
-    uint8_t* d_sflag = nullptr;
+    uint32_t *d_kslot = nullptr, *d_cpar = nullptr, *d_cqp = nullptr;
+    fl::SlotRec* d_rec = nullptr;
+    fl::SlotInfo* d_info = nullptr;
+    uint8_t* d_needl = nullptr;
+    uint64_t* d_push = nullptr;
+    uint32_t tok_cap = 0;
     int *d_bu_done = nullptr, *d_td_need = nullptr, *d_td_done = nullptr;
     uint32_t max_rounds = 0, kahn_min_width = kKahnMinWidth;
     int stamp = 0;
@@ -303,9 +308,10 @@ void free_graph(fl_graph* g) {
                     g->d_flags, g->d_pending, g->d_hgt, g->d_order, g->d_roff, g->d_meta,
                     g->d_sid, g->d_slist, g->d_desig, g->d_sptr0, g->d_sdist0, g->d_sptr1,
                     g->d_sdist1, g->d_cid, g->d_cbot, g->d_clen, g->d_coff, g->d_layout,
-                    g->d_pre, g->d_post, g->d_sflag, g->d_bu_done, g->d_td_need, g->d_td_done,
+                    g->d_pre, g->d_post, g->d_rec, g->d_info, g->d_bu_done, g->d_td_need, g->d_td_done,
                     g->d_slot_chain, g->d_cbas, g->d_el, g->d_cto, g->d_ceo, g->d_perm, g->d_inv,
-                    g->d_post1, g->d_post2, g->d_rtime};
+                    g->d_tokval, g->d_needl, g->d_push, g->d_rtime, g->d_kslot, g->d_cpar,
+                    g->d_cqp};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -413,15 +419,23 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_coff, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_layout, n));
     FL_TRY(dalloc(&g->d_slot_chain, n));
+    FL_TRY(dalloc(&g->d_kslot, n));
+    FL_TRY(dalloc(&g->d_cpar, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_cqp, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_el, n));
     FL_TRY(dalloc(&g->d_cbas, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_cto, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_ceo, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_pre, n));
     FL_TRY(dalloc(&g->d_post, n));
-    FL_TRY(dalloc(&g->d_post1, n));
-    FL_TRY(dalloc(&g->d_post2, n));
-    FL_TRY(dalloc(&g->d_sflag, n));
+    FL_TRY(dalloc(&g->d_rec, n));
+    FL_TRY(dalloc(&g->d_info, n));
+    FL_TRY(dalloc(&g->d_needl, n));
+    FL_TRY(dalloc(&g->d_push, n));
+    // donor lists: each site's list is its cell area plus its donors, so 2n entries
+    // hold every list at once
+    g->tok_cap = (uint32_t)std::min<uint64_t>(2ull * n + 64, 0xfffffff0ull);
+    FL_TRY(dalloc(&g->d_tokval, g->tok_cap));
     FL_TRY(dalloc(&g->d_bu_done, n));
     FL_TRY(dalloc(&g->d_td_need, n));
     FL_TRY(dalloc(&g->d_td_done, n));
@@ -584,7 +598,7 @@ int run_lakes(fl_graph* g) {
 // Drainage areas, response times, elevations on final receivers; *changed.
 // Algorithmic bytes of the kernels that work on the skeleton, whose size is known
 // only once the pass has run (the launch groups were counted with 0 bytes).
-//   bottom-up: pre, post, post1, post2 (32) + flags (1) + area out (8) per slot;
+//   bottom-up: slot record (32) + slot info (8) + area out (8) per slot;
 //              offset, length, bottom id, bottom area, hand-off flag (24) per chain
 //   top-down:  w (8) + flags (1) + t out (8) [+ elevation out (8) with slope limits]
 //              per slot; offset, length, parent t / elevation / outlet, chain outlet
@@ -597,7 +611,7 @@ void account_skeleton(fl_graph* g) {
     const uint32_t longest = g->last_meta[kMetaMaxChain];
     int rounds = 1;
     while (rounds < 32 && (1u << (rounds - 1)) < longest) ++rounds;
-    g->k_bytes[kcSkelUp] += 41.0 * ns + 24.0 * nc;
+    g->k_bytes[kcSkelUp] += 48.0 * ns + 24.0 * nc;
     g->k_bytes[kcSkelDown] += (g->slope ? 25.0 : 17.0) * ns + 56.0 * nc;
     g->k_bytes[kcSkelRank] += 24.0 * ns * rounds;
 }
@@ -655,9 +669,15 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.slope = g->slope;
     a.pre = g->d_pre;
     a.post = g->d_post;
-    a.post1 = g->d_post1;
-    a.post2 = g->d_post2;
-    a.sflag = g->d_sflag;
+    a.kslot = g->d_kslot;
+    a.cpar = g->d_cpar;
+    a.cqp = g->d_cqp;
+    a.rec = g->d_rec;
+    a.info = g->d_info;
+    a.needl = g->d_needl;
+    a.tokval = g->d_tokval;
+    a.tok_cap = g->tok_cap;
+    a.push_to = g->d_push;
     a.bu_done = g->d_bu_done;
     a.td_need = g->d_td_need;
     a.td_done = g->d_td_done;

@@ -38,6 +38,9 @@ def cases():
     yield "negative-operands", 10.0, rng.uniform(-1, 1, 2000)
     yield "non-finite", 1.0, np.array([1.0, np.inf, 2.0, -np.inf, np.nan, 1.0])
     yield "long-river", 0.37, rng.uniform(0.01, 0.02, 40000)
+    # cell areas that lost their low bits to cancellation (granularity 2^-30) added to
+    # a drainage area crossing 2^23 and 2^24: ties with a parity-dependent outcome
+    yield "coarse-areas", 2.0 ** 23 - 3000.0, 1.0 + rng.integers(0, 2 ** 20, 30000) * 2.0 ** -30
     yield "short", 2.5, np.array([0.25])
 
 
