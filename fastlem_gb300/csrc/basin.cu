@@ -743,45 +743,69 @@ struct TopDown {
     const double* tanms;
     const double* rlen;
     const uint8_t* outlet;
-    double* t;
+    TRec* rec;
     double* elev;
-    uint32_t* bas;
     int* flags;
 };
 
-// Response time, basin outlet and elevation of v given its receiver's values.
-// For a root, (tp, ep, o) are ignored.  Returns t_v; writes t, bas, elev.
-__device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t p, double tp,
-                                         uint32_t o, double to, double eo, double ep,
-                                         double* e_out, bool* changed) {
-    double tv;
-    double old_e = __ldcg(&td.elev[v]);
-    if (p == v) {                         // root: t = 0 + (0 + w), o = v
-        tv = plus_zero(plus_zero(td.w[v]));
-        o = td.outlet[v] ? v : kNone;
+__device__ __forceinline__ bool has_outlet(double to) {
+    return (uint64_t)__double_as_longlong(to) != kNoOutletBits;
+}
+
+__device__ __forceinline__ TRec load_rec(const TRec* r) {
+    const double2 a = __ldcg(reinterpret_cast<const double2*>(r));
+    const double2 b = __ldcg(reinterpret_cast<const double2*>(r) + 1);
+    return TRec{a.x, a.y, b.x, b.y};
+}
+
+// Response time and elevation of v from its receiver's record rp (ignored for a root)
+// and v's own inputs (w, uplift, tan of the maximum slope, receiver distance, current
+// elevation, outlet flag).  Writes v's record -- the basin outlet's response time and
+// new elevation carried along, or kNoOutletBits for a basin without an outlet -- and,
+// in a basin with an outlet, its elevation.  Returns t_v.
+__device__ __forceinline__ double settle_own(const TopDown& td, uint32_t v, bool root,
+                                             const TRec& rp, double w, double u, double tn,
+                                             double dist, double old_e, bool is_outlet,
+                                             double* e_out, bool* changed) {
+    double tv, to, eo, ep;
+    bool has_o;
+    if (root) {                           // t = 0 + (0 + w), the outlet is v itself
+        tv = plus_zero(plus_zero(w));
+        has_o = is_outlet;
         to = tv;
         eo = old_e;
         ep = old_e;
     } else {
-        tv = plus_zero(__dadd_rn(tp, td.w[v]));
+        tv = plus_zero(__dadd_rn(rp.t, w));
+        has_o = has_outlet(rp.to);
+        to = rp.to;
+        eo = rp.eo;
+        ep = rp.e;
     }
-    td.t[v] = tv;
-    td.bas[v] = o;
     double ne = old_e;
-    if (o != kNone) {
+    if (has_o) {
         double dt = __dsub_rn(tv, to);
-        ne = __dadd_rn(eo, __dmul_rn(td.uu[v], dt > 0.0 ? dt : 0.0));
-        double tn = td.tanms[v];
+        ne = __dadd_rn(eo, __dmul_rn(u, dt > 0.0 ? dt : 0.0));
         if (!isnan(tn)) {
-            double dist = td.rlen[v];
             double slope = __ddiv_rn(__dsub_rn(ne, ep), dist);
             if (slope > tn) ne = __dadd_rn(ep, __dmul_rn(tn, dist));
         }
         if (ne != old_e) *changed = true;
         td.elev[v] = ne;
     }
+    // below a root the outlet's elevation is its updated one
+    const double to_below = has_o ? to : __longlong_as_double((long long)kNoOutletBits);
+    TRec out{tv, ne, to_below, root ? ne : eo};
+    reinterpret_cast<double2*>(&td.rec[v])[0] = make_double2(out.t, out.e);
+    reinterpret_cast<double2*>(&td.rec[v])[1] = make_double2(out.to, out.eo);
     *e_out = ne;
     return tv;
+}
+
+__device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t p,
+                                         const TRec& rp, double* e_out, bool* changed) {
+    return settle_own(td, v, p == v, rp, td.w[v], td.uu[v], td.tanms[v], td.rlen[v],
+                      __ldcg(&td.elev[v]), td.outlet[v] != 0, e_out, changed);
 }
 
 // Per chain, before the top-down walk (one block): the layout slot of the site it
@@ -808,7 +832,7 @@ __global__ void k_s_chain_roots(TopDown td, const uint32_t* __restrict__ layout,
         const uint32_t p = td.next[v];
         if (p == v) {
             double e;
-            const double tv = settle(td, v, v, 0.0, kNone, 0.0, 0.0, 0.0, &e, &changed);
+            const double tv = settle(td, v, v, TRec{}, &e, &changed);
             tl[off] = tv;
             el[off] = e;
             cpar[c] = c;
@@ -948,9 +972,8 @@ __global__ void k_s_top_down_slope(TopDown td, const uint32_t* __restrict__ layo
                                    const uint32_t* __restrict__ clen,
                                    const uint32_t* __restrict__ cqp,
                                    const uint8_t* __restrict__ needl, double* __restrict__ tl,
-                                   double* __restrict__ el, const uint32_t* __restrict__ cbas,
-                                   const double* __restrict__ cto, const double* __restrict__ ceo,
-                                   int* td_done, int stamp, uint32_t* meta) {
+                                   double* __restrict__ el, int* td_done, int stamp,
+                                   uint32_t* meta) {
     const int lane = threadIdx.x & 31;
     const int wb = threadIdx.x >> 5;
     const uint32_t c = blockIdx.x * kWalkWarps + wb;
@@ -964,12 +987,7 @@ __global__ void k_s_top_down_slope(TopDown td, const uint32_t* __restrict__ layo
     const uint32_t end = off + len;
     uint32_t q = off;
     uint32_t p = td.next[layout[off]];
-    double tp, ep;
-    const uint32_t o = cbas[c];
-    const double to = cto[c], eo = ceo[c];
-    if (cqp[c] == kNone) {
-        tp = tl[off];
-        ep = el[off];
+    if (cqp[c] == kNone) {                 // the root was settled before the walk
         p = layout[off];
         q = off + 1;
     } else {
@@ -985,84 +1003,107 @@ __global__ void k_s_top_down_slope(TopDown td, const uint32_t* __restrict__ layo
         }
         record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
         if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
-        tp = __ldcg(&td.t[p]);
-        ep = __ldcg(&td.elev[p]);
     }
     bool changed = false;
+    TRec rp = load_rec(&td.rec[p]);
     for (; q < end; ++q) {
         const uint32_t v = layout[q];
         double e;
-        tp = settle(td, v, p, tp, o, to, eo, ep, &e, &changed);
+        const double tp = settle(td, v, p, rp, &e, &changed);
+        rp = TRec{tp, e, rp.to, rp.eo};      // the basin outlet's values pass down
         tl[q] = tp;
         el[q] = e;
-        ep = e;
         p = v;
-        if (needl[q]) st_release(&td_done[v], stamp);   // t / elev / bas of v written above
+        if (needl[q]) st_release(&td_done[v], stamp);   // v's record written above
     }
     if (changed) td.flags[kChanged] = 1;
 }
 
-// Skeleton response times and elevations back to site order.
+// Skeleton response times and elevations back to site order (records and elevations;
+// the slope-limited walk wrote its sites itself).
 __global__ void k_s_finish(TopDown td, const uint32_t* __restrict__ layout,
                            const uint32_t* __restrict__ slot_chain, const double* __restrict__ tl,
-                           const double* __restrict__ el, const uint32_t* __restrict__ cbas,
-                           const double* __restrict__ cto, const double* __restrict__ ceo,
-                           bool slope, const uint32_t* meta) {
+                           const uint32_t* __restrict__ cbas, const double* __restrict__ cto,
+                           const double* __restrict__ ceo, const uint32_t* meta) {
     if (td.flags[kError]) return;
     uint32_t ns = meta[kMetaNs];
     bool changed = false;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x) {
         uint32_t v = layout[q];
-        if (td.next[v] == v) continue;     // roots were settled by the walker
-        uint32_t c = slot_chain[q];
-        uint32_t o = cbas[c];
-        double tv = tl[q];
-        td.t[v] = tv;
-        td.bas[v] = o;
-        if (o == kNone) continue;
-        double old_e = td.elev[v];
-        double ne;
-        if (slope) {
-            ne = el[q];
+        if (td.next[v] == v) continue;     // roots were settled before the walk
+        const uint32_t c = slot_chain[q];
+        const bool has_o = cbas[c] != kNone;
+        const double tv = tl[q];
+        const double to = cto[c], eo = ceo[c];
+        double ne = 0.0;
+        if (has_o) {
+            const double old_e = td.elev[v];
+            double dt = __dsub_rn(tv, to);
+            ne = __dadd_rn(eo, __dmul_rn(td.uu[v], dt > 0.0 ? dt : 0.0));
+            if (ne != old_e) changed = true;
+            td.elev[v] = ne;
         } else {
-            double dt = __dsub_rn(tv, cto[c]);
-            ne = __dadd_rn(ceo[c], __dmul_rn(td.uu[v], dt > 0.0 ? dt : 0.0));
+            ne = td.elev[v];
         }
-        if (ne != old_e) changed = true;
-        td.elev[v] = ne;
+        reinterpret_cast<double2*>(&td.rec[v])[0] = make_double2(tv, ne);
+        reinterpret_cast<double2*>(&td.rec[v])[1] =
+            make_double2(has_o ? to : __longlong_as_double((long long)kNoOutletBits), eo);
     }
     block_flag(td.flags, kChanged, changed);
 }
 
-// Top-down over the Kahn rounds, highest round first.
+// Top-down over the Kahn rounds, highest round first, a grid barrier between rounds.
+// After the barrier a site only needs its receiver's record: each thread loads its
+// first site of the next round (id at the start of the round, receiver and own inputs
+// before the barrier), so a narrow round costs about one barrier and one load.
+template <bool kSlope>
 __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
                                const uint32_t* __restrict__ roff, uint64_t* __restrict__ rtime,
                                const uint32_t* meta) {
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
     if (ld_acquire(&td.flags[kError])) return;
-    uint32_t rs = meta[kMetaRStop];
+    const uint32_t rs = meta[kMetaRStop];
     bool changed = false;
     if (gtid == 0) rtime[0] = global_ns();
+    struct Site {
+        uint32_t v, p;
+        double w, u, tn, dist, old_e;
+        bool outlet;
+    };
+    // the slope inputs only with slope limits; the outlet flag only matters for a root
+    auto inputs = [&](uint32_t v, Site& f) {
+        f.v = v;
+        f.p = td.next[v];
+        f.w = td.w[v];
+        f.u = td.uu[v];
+        f.tn = kSlope ? td.tanms[v] : __longlong_as_double(0x7ff8000000000000ll);
+        f.dist = kSlope ? td.rlen[v] : 1.0;
+        f.old_e = __ldcg(&td.elev[v]);
+        f.outlet = false;
+    };
+    Site cur{};
+    bool have = false;
+    if (rs > 0 && roff[rs - 1] + gtid < roff[rs]) {
+        inputs(order[roff[rs - 1] + gtid], cur);
+        have = true;
+    }
     for (uint32_t r = rs; r-- > 0;) {
-        uint32_t b = roff[r], e = roff[r + 1];
+        const uint32_t b = roff[r], e = roff[r + 1];
+        const uint32_t nidx = (r > 0 && roff[r - 1] + gtid < b) ? roff[r - 1] + gtid : kNone;
+        const uint32_t nv = nidx != kNone ? order[nidx] : kNone;   // next round, in flight
         for (uint32_t i = b + gtid; i < e; i += stride) {
-            uint32_t v = order[i];
-            uint32_t p = td.next[v];
-            double tp = 0.0, ep = 0.0, to = 0.0, eo = 0.0;
-            uint32_t o = kNone;
-            if (p != v) {
-                tp = __ldcg(&td.t[p]);
-                ep = __ldcg(&td.elev[p]);
-                o = __ldcg(&td.bas[p]);
-                if (o != kNone) {
-                    to = __ldcg(&td.t[o]);
-                    eo = __ldcg(&td.elev[o]);
-                }
-            }
+            Site f;
+            if (have && i == b + gtid) f = cur;
+            else inputs(order[i], f);
+            const TRec rp = f.p != f.v ? load_rec(&td.rec[f.p]) : TRec{};
+            if (f.p == f.v) f.outlet = td.outlet[f.v] != 0;
             double en;
-            settle(td, v, p, tp, o, to, eo, ep, &en, &changed);
+            settle_own(td, f.v, f.p == f.v, rp, f.w, f.u, f.tn, f.dist, f.old_e, f.outlet, &en,
+                       &changed);
         }
+        have = nv != kNone;
+        if (have) inputs(nv, cur);
         if (!grid_barrier(td.flags)) return;
         if (gtid == 0) rtime[rs - r] = global_ns();
     }
@@ -1131,15 +1172,16 @@ uint32_t walk_capacity() {
 cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz) {
     const uint32_t n = a.n;
     const unsigned nb = (n + kThreads - 1) / kThreads;
-    const unsigned g_kahn = coop_grid((const void*)k_kahn, kRoundBlock, 2);
+    const unsigned g_kahn = coop_grid((const void*)k_kahn, kThreads, 8);
     const unsigned g_rank = coop_grid((const void*)k_s_rank, kRoundBlock, 2);
-    const unsigned g_low = coop_grid((const void*)k_low_top_down, kRoundBlock, 2);
+    const unsigned g_low = coop_grid((const void*)k_low_top_down<false>, kRoundBlock, 2);
+    const unsigned g_low_s = coop_grid((const void*)k_low_top_down<true>, kRoundBlock, 2);
     // ordered compactions: one block range each, two blocks per SM
     const unsigned g_compact = coop_grid((const void*)k_collect_leaves, kRoundBlock, 2);
     const unsigned g_chain = (a.kahn_min_width + kWalkWarps - 1) / kWalkWarps;
     const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
-    TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.t, a.elev, a.bas, a.flags};
+    TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.rec_t, a.elev, a.flags};
     cudaError_t e;
 
     hk.begin(hk.ctx);
@@ -1153,7 +1195,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     // Kahn rounds: order 4 + next 4 + row 8 + area 8 + A 8 + hgt 4 + pending 4 per site,
     // col 4 + next 4 per slot, donor areas 8 per site
     hk.begin(hk.ctx);
-    e = coop_launch(k_kahn, g_kahn, kRoundBlock, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
+    e = coop_launch(k_kahn, g_kahn, kThreads, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
                     a.hgt, a.order, a.roff, a.rtime, a.max_rounds, a.kahn_min_width, a.meta,
                     a.flags);
     hk.end(hk.ctx, kcKahn, 48.0 * n + 8.0 * nnz);
@@ -1224,8 +1266,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
         e = coop_launch(k_s_top_down_slope, g_chain, kWalkWarps * 32, st, td,
                         (const uint32_t*)a.layout, (const uint32_t*)a.coff,
                         (const uint32_t*)a.clen, (const uint32_t*)a.cqp, (const uint8_t*)a.needl,
-                        a.pre, a.el, (const uint32_t*)a.cbas, (const double*)a.cto,
-                        (const double*)a.ceo, a.td_done, a.stamp, a.meta);
+                        a.pre, a.el, a.td_done, a.stamp, a.meta);
     } else {
         e = coop_launch(k_s_top_down, g_chain, kWalkWarps * 32, st, (const int*)a.flags,
                         (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const uint32_t*)a.cqp,
@@ -1235,18 +1276,24 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     if (e != cudaSuccess) return e;
 
     hk.begin(hk.ctx);
-    k_s_finish<<<gs, kThreads, 0, st>>>(td, (const uint32_t*)a.layout,
-                                        (const uint32_t*)a.slot_chain, (const double*)a.pre,
-                                        (const double*)a.el, (const uint32_t*)a.cbas,
-                                        (const double*)a.cto, (const double*)a.ceo, a.slope,
-                                        (const uint32_t*)a.meta);
+    if (!a.slope)
+        k_s_finish<<<gs, kThreads, 0, st>>>(td, (const uint32_t*)a.layout,
+                                            (const uint32_t*)a.slot_chain, (const double*)a.pre,
+                                            (const uint32_t*)a.cbas, (const double*)a.cto,
+                                            (const double*)a.ceo, (const uint32_t*)a.meta);
     hk.end(hk.ctx, kcBasinBuild, 0.0);
 
     // top-down rounds: order 4, next 4, w 8, u 8, tan 8, rlen 8, elev 8+8, t 8, bas 4,
     // parent t/elev/bas 20, outlet t/elev 16 per site
     hk.begin(hk.ctx);
-    e = coop_launch(k_low_top_down, g_low, kRoundBlock, st, td, (const uint32_t*)a.order,
-                    (const uint32_t*)a.roff, a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta);
+    if (a.slope)
+        e = coop_launch(k_low_top_down<true>, g_low_s, kRoundBlock, st, td,
+                        (const uint32_t*)a.order, (const uint32_t*)a.roff,
+                        a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta);
+    else
+        e = coop_launch(k_low_top_down<false>, g_low, kRoundBlock, st, td,
+                        (const uint32_t*)a.order, (const uint32_t*)a.roff,
+                        a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta);
     hk.end(hk.ctx, kcLowDown, 112.0 * n);
     return e;
 }

@@ -76,6 +76,14 @@ struct __align__(8) SlotInfo {
     uint32_t tokoff;
 };
 
+// Per site, once its response time is final: t, elevation, and its basin outlet's
+// response time and (updated) elevation -- everything a donor needs from its receiver
+// in one 32-byte load.  to is kNoOutletBits in a basin without an outlet.
+struct __align__(32) TRec {
+    double t, e, to, eo;
+};
+constexpr uint64_t kNoOutletBits = 0x7ff5000000000000ull;   // a signalling NaN
+
 struct BasinArgs {
     uint32_t n;
     const uint32_t* row;
@@ -88,10 +96,9 @@ struct BasinArgs {
     const double* tanms;
     const uint8_t* outlet;
     double* A;
-    double* t;
+    TRec* rec_t;
     double* w;
     double* elev;
-    uint32_t* bas;
     uint32_t* pending;
     uint32_t* hgt;
     uint32_t* order;

@@ -215,6 +215,12 @@ __global__ void k_lake_flip(uint32_t n, const uint32_t* __restrict__ row,
     rlen[k] = edge_len_or_one(row, col, len, k, nk);
 }
 
+// Response times out of the per-site top-down records (probes).
+__global__ void k_rec_times(uint32_t n, const fl::TRec* __restrict__ rec, double* __restrict__ t) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) t[i] = rec[i].t;
+}
+
 __global__ void k_fill_f64(uint32_t n, double* __restrict__ a, const double* __restrict__ src) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = src ? src[i] : 0.0;
@@ -264,6 +270,7 @@ struct fl_graph {
     int* d_flags = nullptr;
     // basin pass workspace (device)
     uint64_t* d_rtime = nullptr;
+    fl::TRec* d_trec = nullptr;
     uint32_t *d_pending = nullptr, *d_hgt = nullptr, *d_order = nullptr, *d_roff = nullptr,
              *d_meta = nullptr, *d_sid = nullptr, *d_slist = nullptr, *d_desig = nullptr,
              *d_sptr0 = nullptr, *d_sdist0 = nullptr, *d_sptr1 = nullptr, *d_sdist1 = nullptr,
@@ -311,7 +318,7 @@ void free_graph(fl_graph* g) {
                     g->d_pre, g->d_post, g->d_rec, g->d_info, g->d_bu_done, g->d_td_need, g->d_td_done,
                     g->d_slot_chain, g->d_cbas, g->d_el, g->d_cto, g->d_ceo, g->d_perm, g->d_inv,
                     g->d_tokval, g->d_needl, g->d_push, g->d_rtime, g->d_kslot, g->d_cpar,
-                    g->d_cqp};
+                    g->d_cqp, g->d_trec};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -395,6 +402,7 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_sor, n));
     FL_TRY(dalloc(&g->d_outlets, n));
     FL_TRY(dalloc(&g->d_bas, n));
+    FL_TRY(dalloc(&g->d_trec, n));
     FL_TRY(dalloc(&g->d_outlet, n));
     FL_TRY(dalloc(&g->d_best, n));
     FL_TRY(dalloc(&g->d_flags, kNumFlags));
@@ -636,10 +644,9 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.tanms = g->d_tan;
     a.outlet = g->d_outlet;
     a.A = g->d_A;
-    a.t = g->d_t;
+    a.rec_t = g->d_trec;
     a.w = g->d_w;
     a.elev = g->d_elev;
-    a.bas = g->d_bas;
     a.pending = g->d_pending;
     a.hgt = g->d_hgt;
     a.order = g->d_order;
@@ -961,7 +968,8 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
         FL_CU(cudaStreamSynchronize(g->stream));
     }
     if (response_out) {
-        FL_TRY(download_permuted(g, g->d_t, response_out));
+        k_rec_times<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_trec, g->d_w);
+        FL_TRY(download_permuted(g, g->d_w, response_out));
         FL_CU(cudaStreamSynchronize(g->stream));
     }
     if (changed) *changed = ch;
