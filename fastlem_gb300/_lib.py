@@ -30,6 +30,7 @@ EXPORTS = [
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
+    "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
     "fl_probe_rng_f64", "fl_probe_chain_fold", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
 ]
@@ -59,6 +60,11 @@ def lib():
     gen = [vp, c_u32, vp, vp, vp, vp, vp, ctypes.c_int64, vp, P(c_u32)]
     L.fl_generate.argtypes = gen
     L.fl_generate_timed.argtypes = gen + [P(c_dbl), P(c_dbl)]
+    L.fl_batch_create.argtypes = [c_u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, P(vp)]
+    L.fl_graph_num_terrains.argtypes = [vp]
+    L.fl_graph_num_terrains.restype = c_u32
+    L.fl_batch_generate.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, ctypes.c_int64, vp, vp,
+                                    P(c_u32), P(c_dbl), P(c_dbl)]
     L.fl_graph_num_sites.argtypes = [vp]
     L.fl_graph_num_sites.restype = c_u32
     L.fl_graph_num_slots.argtypes = [vp]

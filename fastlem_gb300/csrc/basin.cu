@@ -746,7 +746,15 @@ struct TopDown {
     TRec* rec;
     double* elev;
     int* flags;
+    const uint32_t* tid;   // packed terrains: terrain of each site (else null)
+    int* tchg;             // ... and its "elevation changed" word
 };
+
+// Records that v's elevation changed (per terrain as well when terrains are packed).
+__device__ __forceinline__ void mark_changed(const TopDown& td, uint32_t v, bool* changed) {
+    *changed = true;
+    if (td.tid) td.tchg[td.tid[v]] = 1;
+}
 
 __device__ __forceinline__ bool has_outlet(double to) {
     return (uint64_t)__double_as_longlong(to) != kNoOutletBits;
@@ -790,7 +798,7 @@ __device__ __forceinline__ double settle_own(const TopDown& td, uint32_t v, bool
             double slope = __ddiv_rn(__dsub_rn(ne, ep), dist);
             if (slope > tn) ne = __dadd_rn(ep, __dmul_rn(tn, dist));
         }
-        if (ne != old_e) *changed = true;
+        if (ne != old_e) mark_changed(td, v, changed);
         td.elev[v] = ne;
     }
     // below a root the outlet's elevation is its updated one
@@ -1040,7 +1048,7 @@ __global__ void k_s_finish(TopDown td, const uint32_t* __restrict__ layout,
             const double old_e = td.elev[v];
             double dt = __dsub_rn(tv, to);
             ne = __dadd_rn(eo, __dmul_rn(td.uu[v], dt > 0.0 ? dt : 0.0));
-            if (ne != old_e) changed = true;
+            if (ne != old_e) mark_changed(td, v, &changed);
             td.elev[v] = ne;
         } else {
             ne = td.elev[v];
@@ -1181,7 +1189,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     const unsigned g_chain = (a.kahn_min_width + kWalkWarps - 1) / kWalkWarps;
     const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
-    TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.rec_t, a.elev, a.flags};
+    TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.rec_t, a.elev, a.flags, a.tid, a.tchg};
     cudaError_t e;
 
     hk.begin(hk.ctx);

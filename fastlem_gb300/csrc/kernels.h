@@ -109,6 +109,10 @@ struct BasinArgs {
     uint32_t kahn_min_width;   // also the chain capacity
     uint32_t* meta;
     int* flags;
+    // packed terrains (batched form): terrain of each site, per-terrain "elevation
+    // changed" words; both null for a single terrain
+    const uint32_t* tid;
+    int* tchg;
     // skeleton
     uint32_t* sid;
     uint32_t* slist;

@@ -257,6 +257,16 @@ struct fl_graph {
     // device order: perm[device index] = caller index, inv the reverse
     std::vector<uint32_t> perm, inv;
     uint32_t *d_perm = nullptr, *d_inv = nullptr;
+    // packed terrains (batched form): terrain t owns caller and device sites
+    // [site_off[t], site_off[t+1]) and default outlets [def_off[t], def_off[t+1]);
+    // a single terrain has terrains == 1 and no per-site terrain array
+    uint32_t terrains = 1;
+    std::vector<uint32_t> site_off, def_off;
+    uint32_t noise_n = 0;              // RNG samples a terrain needs (its site count)
+    uint32_t* d_noise_idx = nullptr;   // device site -> its sample (index within its terrain)
+    uint32_t* d_tid = nullptr;
+    int* d_tchg = nullptr;
+    std::vector<int> h_tchg;
     // model (device)
     uint32_t *d_row = nullptr, *d_col = nullptr;
     double *d_len = nullptr, *d_area = nullptr;
@@ -318,7 +328,7 @@ void free_graph(fl_graph* g) {
                     g->d_pre, g->d_post, g->d_rec, g->d_info, g->d_bu_done, g->d_td_need, g->d_td_done,
                     g->d_slot_chain, g->d_cbas, g->d_el, g->d_cto, g->d_ceo, g->d_perm, g->d_inv,
                     g->d_tokval, g->d_needl, g->d_push, g->d_rtime, g->d_kslot, g->d_cpar,
-                    g->d_cqp, g->d_trec};
+                    g->d_cqp, g->d_trec, g->d_noise_idx, g->d_tid, g->d_tchg};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -479,11 +489,18 @@ int device_error(const int* h) {
 
 // Outlet list as generate() resolves it (generator.rs:120-132).
 // Returned in device ids, list order unchanged (the order matters to the lake heap).
+// generator.rs:120-132, per terrain: the sites with is_outlet in ascending order, else
+// the terrain's default outlets (device ids, terrain after terrain).
 std::vector<uint32_t> resolve_outlets(const fl_graph* g, const uint8_t* is_outlet) {
     std::vector<uint32_t> o;
-    for (uint32_t i = 0; i < g->n; ++i)
-        if (is_outlet[i]) o.push_back(g->inv[i]);
-    if (o.empty()) o = g->def_outlets;
+    for (uint32_t t = 0; t < g->terrains; ++t) {
+        const size_t first = o.size();
+        for (uint32_t i = g->site_off[t]; i < g->site_off[t + 1]; ++i)
+            if (is_outlet[i]) o.push_back(g->inv[i]);
+        if (o.size() == first)
+            o.insert(o.end(), g->def_outlets.begin() + g->def_off[t],
+                     g->def_outlets.begin() + g->def_off[t + 1]);
+    }
     return o;
 }
 
@@ -528,16 +545,42 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
     if (need_rank && !g->rank_uploaded) {
         if (!g->rank_valid) {
             g->h_rank.resize(n);
-            if (!fl::lake_heap_rank(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
-                                    outlets.data(), (uint32_t)outlets.size(), g->h_rank.data())) {
-                g_err = "NaN edge length in the lake traversal";
-                return FL_ERR_INVALID_ARGUMENT;
+            if (g->terrains == 1) {
+                if (!fl::lake_heap_rank(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
+                                        outlets.data(), (uint32_t)outlets.size(),
+                                        g->h_rank.data())) {
+                    g_err = "NaN edge length in the lake traversal";
+                    return FL_ERR_INVALID_ARGUMENT;
+                }
+            } else {
+                // each terrain's own traversal (heap ties included), ranks offset by the
+                // terrain's first site: lakes never compare ranks across terrains
+                std::vector<uint32_t> lrow, lcol, lout, lrank;
+                size_t oi = 0;
+                for (uint32_t t = 0; t < g->terrains; ++t) {
+                    const uint32_t a = g->site_off[t], b = g->site_off[t + 1], m = b - a;
+                    const uint32_t s0 = g->h_row[a];
+                    lrow.resize(m + 1);
+                    for (uint32_t j = 0; j <= m; ++j) lrow[j] = g->h_row[a + j] - s0;
+                    lcol.resize(g->h_row[b] - s0);
+                    for (uint32_t s = s0; s < g->h_row[b]; ++s) lcol[s - s0] = g->h_col[s] - a;
+                    lout.clear();
+                    while (oi < outlets.size() && outlets[oi] < b) lout.push_back(outlets[oi++] - a);
+                    lrank.resize(m);
+                    if (!fl::lake_heap_rank(m, lrow.data(), lcol.data(), g->h_len.data() + s0,
+                                            lout.data(), (uint32_t)lout.size(), lrank.data())) {
+                        g_err = "NaN edge length in the lake traversal";
+                        return FL_ERR_INVALID_ARGUMENT;
+                    }
+                    for (uint32_t j = 0; j < m; ++j)
+                        g->h_rank[a + j] = lrank[j] == kNone ? kNone : a + lrank[j];
+                }
             }
             g->rank_valid = true;
         }
         std::vector<uint32_t> sor(n, kNone);
         for (uint32_t v = 0; v < n; ++v)
-            if (g->h_rank[v] != kNone) sor[g->h_rank[v]] = v;
+            if (g->h_rank[v] != kNone && g->h_rank[v] < n) sor[g->h_rank[v]] = v;
         FL_CU(cudaMemcpyAsync(g->d_rank, g->h_rank.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
         FL_CU(cudaMemcpyAsync(g->d_sor, sor.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
         FL_CU(cudaStreamSynchronize(g->stream));
@@ -656,6 +699,8 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.kahn_min_width = g->kahn_min_width;
     a.meta = g->d_meta;
     a.flags = g->d_flags;
+    a.tid = g->d_tid;
+    a.tchg = g->d_tchg;
     a.sid = g->d_sid;
     a.slist = g->d_slist;
     a.desig = g->d_desig;
@@ -736,7 +781,7 @@ int upload_params(fl_graph* g, const double* base, const double* k, const double
 int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const double* k,
                   const double* u, const uint8_t* is_outlet, const double* max_slope,
                   int64_t max_iter, double* out_elev, uint32_t* out_iters, double* loop_ms,
-                  double* total_ms) {
+                  double* total_ms, uint32_t* terrain_iters = nullptr) {
     g_err.clear();
     if (!g) return FL_ERR_MODEL_NOT_SET;
     if (!base || !k || !u || !is_outlet) return FL_ERR_PARAMETERS_NOT_SET;
@@ -750,11 +795,12 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     FL_TRY(set_outlets(g, outlets, false));
     // all status words, including the grid barrier's, start from zero
     FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
-    FL_LAUNCH(g, kcNoise, 8.0 * n,
-              k_noise<<<blocks_for((n + 7) / 8), kThreads, 0, g->stream>>>(n, g->d_w));
+    // every terrain draws its own StdRng::seed_from_u64(0) stream, sample i for its site i
+    FL_LAUNCH(g, kcNoise, 8.0 * g->noise_n,
+              k_noise<<<blocks_for((g->noise_n + 7) / 8), kThreads, 0, g->stream>>>(g->noise_n, g->d_w));
     FL_LAUNCH(g, kcNoise, 28.0 * n,
               k_initial_elevation<<<blocks_for(n), kThreads, 0, g->stream>>>(
-                  n, g->d_perm, g->d_base, g->d_w, g->d_elev));
+                  n, g->d_noise_idx ? g->d_noise_idx : g->d_perm, g->d_base, g->d_w, g->d_elev));
     // previous-iteration drainage areas steer the skeleton's chain choice; start from
     // the cell areas
     FL_LAUNCH(g, kcMisc, 16.0 * n,
@@ -764,6 +810,9 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     if (max_iter > 0xffffffffll) max_iter = 0xffffffffll;
     uint64_t limit = max_iter < 0 ? 0xffffffffull : (uint64_t)max_iter;
     uint32_t iters = 0;
+    // a terrain alone stops at its first iteration without a change; packed with others
+    // it keeps iterating at a fixed point, so its count is that first unchanged iteration
+    std::vector<uint32_t> t_iters(g->terrains, 0);
     for (uint64_t it = 0; it < limit; ++it) {
         ++iters;
         int has_lake = 0, changed = 0;
@@ -773,9 +822,21 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
             FL_TRY(run_labels(g));
             FL_TRY(run_lakes(g));
         }
+        if (g->d_tchg)
+            FL_CU(cudaMemsetAsync(g->d_tchg, 0, g->terrains * sizeof(int), g->stream));
         FL_TRY(run_basin_pass(g, &changed));
+        if (g->d_tchg) {
+            FL_CU(cudaMemcpyAsync(g->h_tchg.data(), g->d_tchg, g->terrains * sizeof(int),
+                                  cudaMemcpyDeviceToHost, g->stream));
+            FL_CU(cudaStreamSynchronize(g->stream));
+            for (uint32_t t = 0; t < g->terrains; ++t)
+                if (!t_iters[t] && !g->h_tchg[t]) t_iters[t] = iters;
+        }
         if (!changed) break;
     }
+    if (terrain_iters)
+        for (uint32_t t = 0; t < g->terrains; ++t)
+            terrain_iters[t] = t_iters[t] ? t_iters[t] : iters;
     FL_CU(cudaEventRecord(g->ev1, g->stream));
     FL_TRY(download_permuted(g, g->d_elev, out_elev));
     FL_CU(cudaStreamSynchronize(g->stream));
@@ -800,41 +861,84 @@ extern "C" {
 
 const char* fl_last_error(void) { return g_err.c_str(); }
 
-int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
-                    const double* area, const uint32_t* default_outlets, uint32_t n_default,
-                    const double* xs, const double* ys, fl_graph** out) {
+}  // extern "C"
+
+namespace {
+
+// A model on the current device.  k_terr > 1 packs terrains: site_off / def_off give
+// each terrain's caller sites and default outlets, no edge may cross terrains, and each
+// terrain is ordered along its own Hilbert curve (coordinates are per terrain).
+int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
+                 const double* area, const uint32_t* default_outlets, uint32_t n_default,
+                 const double* xs, const double* ys, uint32_t k_terr, const uint32_t* site_off,
+                 const uint32_t* def_off, fl_graph** out) {
     g_err.clear();
     if (!out || !row_ptr || (!col && n) || !area || (n_default && !default_outlets) || n == 0 ||
-        n >= kNone) {
+        n >= kNone || k_terr == 0 || (k_terr > 1 && (!site_off || !def_off))) {
         g_err = "invalid graph arguments";
         return FL_ERR_INVALID_ARGUMENT;
     }
     *out = nullptr;
+    std::vector<uint32_t> so(k_terr + 1), dof(k_terr + 1);
+    if (k_terr == 1) {
+        so = {0, n};
+        dof = {0, n_default};
+    } else {
+        for (uint32_t t = 0; t <= k_terr; ++t) {
+            so[t] = site_off[t];
+            dof[t] = def_off[t];
+        }
+        if (so[0] != 0 || so[k_terr] != n || dof[0] != 0 || dof[k_terr] != n_default) {
+            g_err = "terrain offsets do not cover the sites / default outlets";
+            return FL_ERR_INVALID_ARGUMENT;
+        }
+        for (uint32_t t = 0; t < k_terr; ++t)
+            if (so[t + 1] <= so[t] || dof[t + 1] < dof[t]) {
+                g_err = "terrain offsets not increasing (empty terrain?)";
+                return FL_ERR_INVALID_ARGUMENT;
+            }
+    }
     uint64_t nnz = row_ptr[n];
     if (row_ptr[0] != 0) { g_err = "row_ptr[0] != 0"; return FL_ERR_INVALID_ARGUMENT; }
     for (uint32_t i = 0; i < n; ++i)
         if (row_ptr[i + 1] < row_ptr[i]) { g_err = "row_ptr not monotone"; return FL_ERR_INVALID_ARGUMENT; }
     for (uint64_t s = 0; s < nnz; ++s)
         if (col[s] >= n || std::isnan(len[s])) { g_err = "column out of range or NaN length"; return FL_ERR_INVALID_ARGUMENT; }
-    {
-        std::vector<uint8_t> seen(n, 0);
-        for (uint32_t i = 0; i < n_default; ++i) {
-            if (default_outlets[i] >= n || seen[default_outlets[i]]) {
-                g_err = "default outlet out of range or repeated";
+    for (uint32_t t = 0; t < k_terr; ++t) {
+        for (uint32_t i = so[t]; i < so[t + 1]; ++i)
+            for (uint32_t s = row_ptr[i]; s < row_ptr[i + 1]; ++s)
+                if (col[s] < so[t] || col[s] >= so[t + 1]) {
+                    g_err = "an edge crosses two terrains";
+                    return FL_ERR_INVALID_ARGUMENT;
+                }
+        std::vector<uint8_t> seen(so[t + 1] - so[t], 0);
+        for (uint32_t i = dof[t]; i < dof[t + 1]; ++i) {
+            const uint32_t o = default_outlets[i];
+            if (o < so[t] || o >= so[t + 1] || seen[o - so[t]]) {
+                g_err = "default outlet out of its terrain's range or repeated";
                 return FL_ERR_INVALID_ARGUMENT;
             }
-            seen[default_outlets[i]] = 1;
+            seen[o - so[t]] = 1;
         }
     }
     fl_graph* g = new fl_graph();
     if (cudaGetDevice(&g->device) != cudaSuccess) g->device = 0;
     g->n = n;
     g->nnz = nnz;
-    if (xs && ys) {
-        fl::hilbert_order(n, xs, ys, g->perm);
-    } else {
-        g->perm.resize(n);
-        for (uint32_t i = 0; i < n; ++i) g->perm[i] = i;
+    g->terrains = k_terr;
+    g->site_off = so;
+    g->def_off = dof;
+    g->perm.resize(n);
+    for (uint32_t t = 0; t < k_terr; ++t) {
+        const uint32_t a = so[t], m = so[t + 1] - so[t];
+        g->noise_n = std::max(g->noise_n, m);
+        if (xs && ys) {
+            std::vector<uint32_t> lp;
+            fl::hilbert_order(m, xs + a, ys + a, lp);
+            for (uint32_t j = 0; j < m; ++j) g->perm[a + j] = a + lp[j];
+        } else {
+            for (uint32_t j = 0; j < m; ++j) g->perm[a + j] = a + j;
+        }
     }
     g->inv.resize(n);
     for (uint32_t j = 0; j < n; ++j) g->inv[g->perm[j]] = j;
@@ -864,8 +968,61 @@ int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, co
         g_err = "graph upload failed";
         return fail(FL_ERR_CUDA);
     }
+    if (k_terr > 1) {
+        // per device site: its sample of its terrain's noise stream, and its terrain
+        std::vector<uint32_t> nidx(n), tid(n);
+        for (uint32_t t = 0; t < k_terr; ++t)
+            for (uint32_t j = so[t]; j < so[t + 1]; ++j) {
+                nidx[j] = g->perm[j] - so[t];
+                tid[j] = t;
+            }
+        g->h_tchg.assign(k_terr, 0);
+        if ((rc = dalloc(&g->d_noise_idx, n)) || (rc = dalloc(&g->d_tid, n)) ||
+            (rc = dalloc(&g->d_tchg, k_terr)))
+            return fail(rc);
+        if (cudaMemcpy(g->d_noise_idx, nidx.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(g->d_tid, tid.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) {
+            g_err = "graph upload failed";
+            return fail(FL_ERR_CUDA);
+        }
+    }
     *out = g;
     return FL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fl_graph_create(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
+                    const double* area, const uint32_t* default_outlets, uint32_t n_default,
+                    const double* xs, const double* ys, fl_graph** out) {
+    return create_graph(n, row_ptr, col, len, area, default_outlets, n_default, xs, ys, 1,
+                        nullptr, nullptr, out);
+}
+
+int fl_batch_create(uint32_t terrains, const uint32_t* site_off, const uint32_t* row_ptr,
+                    const uint32_t* col, const double* len, const double* area,
+                    const uint32_t* def_off, const uint32_t* default_outlets, const double* xs,
+                    const double* ys, fl_graph** out) {
+    if (!site_off || !def_off || terrains == 0) {
+        g_err = "invalid batch arguments";
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    return create_graph(site_off[terrains], row_ptr, col, len, area, default_outlets,
+                        def_off[terrains], xs, ys, terrains, site_off, def_off, out);
+}
+
+uint32_t fl_graph_num_terrains(const fl_graph* g) { return g ? g->terrains : 0; }
+
+int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
+                      const double* erodibility, const double* uplift, const uint8_t* is_outlet,
+                      const double* max_slope, int64_t max_iteration, double* out_elev,
+                      uint32_t* out_terrain_iterations, uint32_t* out_iterations,
+                      double* loop_ms, double* total_ms) {
+    return generate_impl(g, n_params, base, erodibility, uplift, is_outlet, max_slope,
+                         max_iteration, out_elev, out_iterations, loop_ms, total_ms,
+                         out_terrain_iterations);
 }
 
 void fl_graph_destroy(fl_graph* g) { free_graph(g); }

@@ -13,6 +13,7 @@ from StdRng::seed_from_u64(seed).  `scale` shrinks a config's site count and box
 together (same density) for parity runs at reduced size.
 """
 import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -119,3 +120,43 @@ def sixteen_million(scale=1.0):
 
 
 CONFIGS = {"small": small, "1m": one_million, "16m": sixteen_million}
+
+
+def _build_many(specs, threads):
+    """Models for (n, side, seed) specs, built on a thread pool (the builder's C++
+    calls release the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        return list(ex.map(lambda s: build_model(s[0], s[1], s[2], 0), specs))
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    models: list
+    params: list
+    config: dict = field(default_factory=dict)
+
+    @property
+    def sites(self):
+        return sum(m.num() for m in self.models)
+
+
+def batched(count=512, lo=4096, hi=262144, seed=3, threads=None):
+    """512 independent terrains, site counts log-uniform in [4096, 262144] (seed 3), each
+    uniform-random in its own square of side sqrt(n), border outlets within 2% of the
+    side, log-normal(0, 0.5) erodibility."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(math.log(lo), math.log(hi), count)).astype(np.int64)
+    seeds = rng.integers(1, 2**31, count)
+    specs = [(int(n), math.sqrt(n), int(sd)) for n, sd in zip(ns, seeds)]
+    models = _build_many(specs, threads or os.cpu_count() or 1)
+    params = []
+    for (n, side, sd), m in zip(specs, models):
+        r = np.random.default_rng(int(sd) + 1)
+        k = np.exp(r.normal(0.0, 0.5, n))
+        params.append(ParameterArrays(n, erodibility=k, is_outlet=border_outlets(m, side, 0.02 * side)))
+    return BatchWorkload("batched", models, params,
+                         {"terrains": count, "sites": int(ns.sum()), "n_range": [lo, hi],
+                          "seed": seed, "outlets": "border<2% of side",
+                          "erodibility": "lognormal(0,0.5)"})

@@ -94,6 +94,34 @@ int fl_generate_timed(fl_graph* g, uint32_t n_params, const double* base,
 uint32_t fl_graph_num_sites(const fl_graph* g);
 uint64_t fl_graph_num_slots(const fl_graph* g);
 
+/* ---- batched form (no fastlem counterpart: many generate() calls in one solve) ----
+ *
+ * `terrains` independent models packed into one graph with global site ids: terrain t
+ * owns sites [site_off[t], site_off[t+1]) (its CSR rows, areas, coordinates) and
+ * default outlets [def_off[t], def_off[t+1]) of `default_outlets`; no edge may cross
+ * terrains.  xs / ys are each terrain's own coordinates (or NULL).  Each terrain is
+ * solved exactly as fl_generate would solve it alone: its own outlet resolution
+ * (generator.rs:120-132), its own StdRng noise stream (generator.rs:134-138) and its
+ * own lake-heap order, so its elevations are bit-identical to a solo solve. */
+int fl_batch_create(uint32_t terrains, const uint32_t* site_off, const uint32_t* row_ptr,
+                    const uint32_t* col, const double* len, const double* area,
+                    const uint32_t* def_off, const uint32_t* default_outlets, const double* xs,
+                    const double* ys, fl_graph** out);
+
+/* Number of packed terrains of a model (1 for fl_graph_create models). */
+uint32_t fl_graph_num_terrains(const fl_graph* g);
+
+/* generate() for every packed terrain at once: per-site parameters over all sites, one
+ * max_iteration for all.  out_terrain_iterations[t] = the loop bodies terrain t would
+ * have run alone (its first iteration without an elevation change, or the limit);
+ * out_iterations = loop bodies of the packed solve (the largest).  loop_ms / total_ms
+ * as in fl_generate_timed; any of the last four pointers may be NULL. */
+int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
+                      const double* erodibility, const double* uplift, const uint8_t* is_outlet,
+                      const double* max_slope, int64_t max_iteration, double* out_elev,
+                      uint32_t* out_terrain_iterations, uint32_t* out_iterations,
+                      double* loop_ms, double* total_ms);
+
 /* Message for the last error on this thread ("" when none). */
 const char* fl_last_error(void);
 
