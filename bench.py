@@ -39,7 +39,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="16m", choices=["small", "1m", "16m", "batched"])
+    ap.add_argument("--config", default="16m", choices=["small", "1m", "16m", "batched", "served"])
+    ap.add_argument("--requests", type=int, default=64, help="served: requests in the stream")
+    ap.add_argument("--slots", type=int, default=4, help="served: concurrent requests")
+    ap.add_argument("--serve-iters", type=int, default=64,
+                    help="served: set_max_iteration per request (fastlem's loop may not settle)")
     ap.add_argument("--terrains", type=int, default=512, help="batched: terrain count")
     ap.add_argument("--batch-iters", type=int, default=256,
                     help="batched: set_max_iteration per terrain (fastlem's loop may not settle)")
@@ -380,11 +384,96 @@ def bench_batched(args, d):
     print(json.dumps(line), flush=True)
 
 
+def bench_served(args, d):
+    """C5: a Poisson stream of generate() requests (200 req/s, 16,384-4,194,304 sites)
+    replayed in real time, once through the server (concurrent requests, resident
+    models, 120 GB HBM admission budget) and once one request at a time through the
+    plain path; latency = completion - arrival.  Both start cold (each request's graph
+    is uploaded by its first solve)."""
+    from fastlem_gb300 import TerrainGenerator, build as fb, workloads
+    from fastlem_gb300.serve import TerrainServer
+    fb.build()
+    from fastlem_gb300 import _lib
+    _lib.check(_lib.lib().fl_select_device(d.local))
+    t0 = time.time()
+    w = workloads.served(count=args.requests)
+    build_s = time.time() - t0
+    R = len(w.models)
+    cap = args.serve_iters
+    # CUDA context and library warm-up on a throw-away model
+    tiny = workloads.small(scale=0.1)
+    TerrainGenerator.default().set_model(tiny.model).set_parameters(tiny.params).generate()
+
+    def replay(start_one, finish_all):
+        t0 = time.perf_counter()
+        handles = []
+        for i in range(R):
+            now = time.perf_counter() - t0
+            if now < w.arrivals[i]:
+                time.sleep(w.arrivals[i] - now)
+            handles.append(start_one(i, t0))
+        res = finish_all(handles, t0)
+        return res, time.perf_counter() - t0
+
+    # sequential plain GPU path
+    gens = [TerrainGenerator.default().set_model(m).set_parameters(p).set_max_iteration(cap)
+            for m, p in zip(w.models, w.params)]
+    def seq_one(i, t0):
+        e = gens[i].generate().elevations()
+        return e, (time.perf_counter() - t0 - w.arrivals[i]) * 1000, gens[i].last_iterations
+    seq, seq_span = replay(seq_one, lambda hs, t0: hs)
+    # served
+    with ClockSampler(max(1, args.gpus)) as clocks:
+        with TerrainServer(hbm_budget_bytes=120 * 10**9, slots=args.slots) as srv:
+            ids = [srv.add_model(m) for m in w.models]
+            served, span = replay(lambda i, t0: srv.submit(ids[i], w.params[i], cap),
+                                  lambda hs, t0: [srv.wait(h) for h in hs])
+            stats = srv.stats()
+    if d.rank != 0:
+        return
+    lat = np.array([info["latency_ms"] for _, info in served])
+    seq_lat = np.array([l for _, l, _ in seq])
+    identical = all(np.array_equal(a.view(np.uint64), t.elevations().view(np.uint64))
+                    for (a, _, _), (t, _) in zip(seq, served))
+    iters = np.array([info["iterations"] for _, info in served])
+    site_iters = int(sum(m.num() * int(i) for m, i in zip(w.models, iters)))
+    value = R / span
+    line = {
+        "metric": "served terrains/s and p99 latency (Poisson 200 req/s, 16,384-4,194,304 sites)",
+        "value": value, "unit": "terrains/s", "n_gpus": args.gpus, "steps": 1, "warmup": 1,
+        "ms_per_step": span * 1000, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"served: {R} requests, Poisson {w.config['rate_per_s']:g}/s seed 5, "
+                               f"n log-uniform [16384, 4194304], {w.config['sites']:,} sites, "
+                               f"per-request erodibility field, border outlets 2%, until an "
+                               f"iteration changes nothing or {cap} iterations",
+                   "slots": args.slots, "hbm_budget_gb": 120,
+                   "requests_at_iteration_cap": int((iters >= cap).sum()),
+                   "site_iterations": site_iters, "graph_build_s": round(build_s, 1)},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(lat.max())},
+        "e2e": {"value": value, "unit": "terrains/s",
+                "h2d_bytes_per_step": int(sum(m.num() * 25 for m in w.models)),
+                "d2h_bytes_per_step": int(sum(m.num() * 8 for m in w.models))},
+        "sequential_plain": {"terrains_per_s": R / seq_span,
+                             "latency_ms": {"p50": float(np.percentile(seq_lat, 50)),
+                                            "p99": float(np.percentile(seq_lat, 99))}},
+        "speedup_vs_sequential": (R / span) / (R / seq_span),
+        "identical_to_plain": identical,
+        "server": stats,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     d = Dist()
     if args.config == "batched" and args.impl != "reference":
         bench_batched(args, d)
+        return
+    if args.config == "served" and args.impl != "reference":
+        bench_served(args, d)
         return
     if args.impl == "reference":
         bench_reference(args, d)

@@ -30,7 +30,9 @@ EXPORTS = [
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
-    "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate",
+    "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate", "fl_graph_device_bytes",
+    "fl_server_create", "fl_server_add_model", "fl_server_submit", "fl_server_wait",
+    "fl_server_stats", "fl_server_destroy",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
     "fl_probe_rng_f64", "fl_probe_chain_fold", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
 ]
@@ -63,6 +65,15 @@ def lib():
     L.fl_batch_create.argtypes = [c_u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, P(vp)]
     L.fl_graph_num_terrains.argtypes = [vp]
     L.fl_graph_num_terrains.restype = c_u32
+    L.fl_graph_device_bytes.argtypes = [vp]
+    L.fl_graph_device_bytes.restype = c_u64
+    L.fl_server_create.argtypes = [c_u64, c_u32, P(vp)]
+    L.fl_server_add_model.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, c_u32, vp, vp, P(c_u32)]
+    L.fl_server_submit.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, ctypes.c_int64, vp, P(c_u64)]
+    L.fl_server_wait.argtypes = [vp, c_u64, P(c_u32), P(c_dbl), P(c_dbl), P(c_dbl)]
+    L.fl_server_stats.argtypes = [vp, vp, c_u32]
+    L.fl_server_destroy.argtypes = [vp]
+    L.fl_server_destroy.restype = None
     L.fl_batch_generate.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, ctypes.c_int64, vp, vp,
                                     P(c_u32), P(c_dbl), P(c_dbl)]
     L.fl_graph_num_sites.argtypes = [vp]

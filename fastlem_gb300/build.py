@@ -22,7 +22,7 @@ LIB = os.path.join(OUT_DIR, "libfastlem_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_SOURCES = ["solver.cu", "receivers.cu", "basin.cu", "noalloc.cu"]
-CXX_SOURCES = ["builder.cpp", "prim_rank.cpp", "ordering.cpp"]
+CXX_SOURCES = ["builder.cpp", "prim_rank.cpp", "ordering.cpp", "server.cpp"]
 HEADERS = ["rng.h", "common.cuh", "kernels.h", "fold.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -66,12 +66,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append(([nvcc, *NVCC_FLAGS, "-c", s, "-o", o], o + ".log"))
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
     for src in CXX_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT_DIR, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append((["g++", *CXX_FLAGS, "-c", s, "-o", o], o + ".log"))
+            jobs.append((["g++", *CXX_FLAGS, "-I", cuda_inc, "-c", s, "-o", o], o + ".log"))
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(lambda j: _run(*j), jobs))
     if force or jobs or _stale(LIB, objs):

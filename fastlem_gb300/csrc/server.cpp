@@ -1,0 +1,338 @@
+// server.cpp -- served form: a request loop of generate() calls of different sizes.
+//
+// fastlem answers one TerrainGenerator::generate() call at a time
+// (lem/generator.rs:90-213).  The server takes such calls as they arrive, for models
+// registered once, and runs several at once on one GPU:
+//   * every registered model keeps a host copy; a request needs a device instance of
+//     its model (an fl_graph: graph plus workspace), created on admission and kept
+//     resident afterwards for the next request on the same model;
+//   * `slots` worker threads each run one request at a time on the instance's own CUDA
+//     stream, so the kernels of concurrent requests overlap on the device;
+//   * admission is first-come first-served: the oldest waiting request starts when a
+//     worker is free and its instance is idle or fits the HBM budget, after evicting
+//     idle instances (least recently used first); requests behind it wait, so a large
+//     request is never starved by smaller ones;
+//   * each request records its queueing time, solve time and latency.
+// A request's result is exactly fl_generate's on its own: instances share nothing.
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <list>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "fastlem_gb300.h"
+#include "kernels.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct Model {
+    uint32_t n = 0;
+    std::vector<uint32_t> row, col, outlets;
+    std::vector<double> len, area, xs, ys;
+    bool coords = false;
+    uint64_t bytes = 0;                 // device bytes of one instance (measured)
+    std::vector<fl_graph*> idle;        // resident instances, most recently used last
+    uint32_t busy = 0;
+};
+
+struct Request {
+    uint64_t id = 0;
+    uint32_t model = 0;
+    std::vector<double> base, k, u, slope;
+    std::vector<uint8_t> outlet;
+    bool has_slope = false;
+    int64_t max_iter = -1;
+    double* out = nullptr;
+    Clock::time_point arrived, started, finished;
+    uint32_t iterations = 0;
+    int status = FL_OK;
+    std::string error;
+    bool done = false;
+};
+
+}  // namespace
+
+struct fl_server {
+    uint64_t budget = 0;
+    uint64_t used = 0;                  // device bytes of all live instances
+    uint32_t slots = 0;
+    int device = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::vector<std::unique_ptr<Model>> models;
+    std::deque<Request*> queue;
+    std::map<uint64_t, std::unique_ptr<Request>> requests;
+    std::list<std::pair<uint32_t, fl_graph*>> lru;   // idle instances, oldest first
+    std::vector<std::thread> workers;
+    uint64_t next_id = 1;
+    bool stop = false;
+    // statistics
+    uint32_t active = 0, peak_active = 0;
+    uint64_t peak_used = 0, created = 0, evicted = 0, completed = 0;
+};
+
+namespace {
+
+// An instance's device footprint before it exists: the measured size of an earlier
+// instance of the same model, else a bound from the site and slot counts (an instance
+// allocates about 330 B per site, 12 B per adjacency slot and under 1 MiB besides).
+uint64_t footprint(const Model& m) {
+    if (m.bytes) return m.bytes;
+    return 400ull * m.n + 16ull * m.col.size() + (1ull << 20);
+}
+
+void drop_idle(fl_server* s, uint32_t model, fl_graph* g) {
+    s->lru.remove(std::make_pair(model, g));
+    auto& v = s->models[model]->idle;
+    v.erase(std::remove(v.begin(), v.end(), g), v.end());
+}
+
+// With the lock held: can the head request start now?  Takes an idle instance
+// (*inst) or reserves budget for a new one (*reserve), evicting idle instances of
+// other models as needed (collected in *evict, destroyed outside the lock).
+bool admit(fl_server* s, Request* r, fl_graph** inst, uint64_t* reserve,
+           std::vector<fl_graph*>* evict) {
+    Model& m = *s->models[r->model];
+    if (!m.idle.empty()) {
+        *inst = m.idle.back();
+        drop_idle(s, r->model, *inst);
+        return true;
+    }
+    const uint64_t need = footprint(m);
+    uint64_t freeable = 0;
+    for (auto& e : s->lru) freeable += s->models[e.first]->bytes;
+    if (s->used + need > s->budget + freeable) return false;
+    while (s->used + need > s->budget && !s->lru.empty()) {
+        auto e = s->lru.front();
+        s->lru.pop_front();
+        auto& v = s->models[e.first]->idle;
+        v.erase(std::remove(v.begin(), v.end(), e.second), v.end());
+        s->used -= s->models[e.first]->bytes;
+        evict->push_back(e.second);
+        s->evicted++;
+    }
+    s->used += need;
+    *reserve = need;
+    *inst = nullptr;
+    return true;
+}
+
+void worker(fl_server* s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    while (true) {
+        Request* r = nullptr;
+        fl_graph* inst = nullptr;
+        uint64_t reserve = 0;
+        std::vector<fl_graph*> evict;
+        s->cv_work.wait(lk, [&] {
+            if (s->stop) return true;
+            if (s->queue.empty()) return false;
+            return admit(s, s->queue.front(), &inst, &reserve, &evict);
+        });
+        if (s->stop) return;
+        r = s->queue.front();
+        s->queue.pop_front();
+        Model& m = *s->models[r->model];
+        m.busy++;
+        s->active++;
+        s->peak_active = std::max(s->peak_active, s->active);
+        r->started = Clock::now();
+        lk.unlock();
+        s->cv_work.notify_all();           // the next request may fit as well
+        for (fl_graph* g : evict) fl_graph_destroy(g);
+        int rc = FL_OK;
+        std::string err;
+        if (!inst) {
+            rc = fl_graph_create(m.n, m.row.data(), m.col.data(), m.len.data(), m.area.data(),
+                                 m.outlets.data(), (uint32_t)m.outlets.size(),
+                                 m.coords ? m.xs.data() : nullptr,
+                                 m.coords ? m.ys.data() : nullptr, &inst);
+            if (rc != FL_OK) err = fl_last_error();
+        }
+        uint64_t real = inst ? fl_graph_device_bytes(inst) : 0;
+        if (rc == FL_OK) {
+            rc = fl_generate(inst, m.n, r->base.data(), r->k.data(), r->u.data(),
+                             r->outlet.data(), r->has_slope ? r->slope.data() : nullptr,
+                             r->max_iter, r->out, &r->iterations);
+            if (rc != FL_OK) err = fl_last_error();
+        }
+        lk.lock();
+        if (reserve) {                      // the reservation becomes the measured size
+            s->used -= reserve;
+            if (inst) {
+                s->used += real;
+                m.bytes = real;
+                s->created++;
+            }
+        }
+        s->peak_used = std::max(s->peak_used, s->used);
+        if (inst) {
+            if (rc == FL_OK) {
+                m.idle.push_back(inst);
+                s->lru.emplace_back(r->model, inst);
+            } else {                        // a failed instance is not reused
+                s->used -= m.bytes;
+                lk.unlock();
+                fl_graph_destroy(inst);
+                lk.lock();
+            }
+        }
+        m.busy--;
+        s->active--;
+        r->status = rc;
+        r->error = err;
+        r->finished = Clock::now();
+        r->done = true;
+        s->completed++;
+        s->cv_done.notify_all();
+        s->cv_work.notify_all();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fl_server_create(uint64_t hbm_budget_bytes, uint32_t slots, fl_server** out) {
+    if (!out || slots == 0 || hbm_budget_bytes == 0) {
+        fl::set_last_error("fl_server_create: invalid arguments");
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    fl_server* s = new fl_server();
+    s->budget = hbm_budget_bytes;
+    s->slots = slots;
+    if (cudaGetDevice(&s->device) != cudaSuccess) s->device = 0;
+    for (uint32_t i = 0; i < slots; ++i) s->workers.emplace_back(worker, s);
+    *out = s;
+    return FL_OK;
+}
+
+int fl_server_add_model(fl_server* s, uint32_t n, const uint32_t* row_ptr, const uint32_t* col,
+                        const double* len, const double* area, const uint32_t* default_outlets,
+                        uint32_t n_default, const double* xs, const double* ys,
+                        uint32_t* model_id) {
+    if (!s || !row_ptr || !area || !model_id || n == 0 || (n_default && !default_outlets)) {
+        fl::set_last_error("fl_server_add_model: invalid arguments");
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    auto m = std::make_unique<Model>();
+    m->n = n;
+    m->row.assign(row_ptr, row_ptr + n + 1);
+    const uint64_t nnz = row_ptr[n];
+    m->col.assign(col, col + nnz);
+    m->len.assign(len, len + nnz);
+    m->area.assign(area, area + n);
+    m->outlets.assign(default_outlets, default_outlets + n_default);
+    if (xs && ys) {
+        m->coords = true;
+        m->xs.assign(xs, xs + n);
+        m->ys.assign(ys, ys + n);
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    *model_id = (uint32_t)s->models.size();
+    s->models.push_back(std::move(m));
+    return FL_OK;
+}
+
+int fl_server_submit(fl_server* s, uint32_t model_id, const double* base,
+                     const double* erodibility, const double* uplift, const uint8_t* is_outlet,
+                     const double* max_slope, int64_t max_iteration, double* out_elev,
+                     uint64_t* ticket) {
+    if (!s || !ticket) return FL_ERR_INVALID_ARGUMENT;
+    if (!base || !erodibility || !uplift || !is_outlet) return FL_ERR_PARAMETERS_NOT_SET;
+    if (!out_elev) return FL_ERR_INVALID_ARGUMENT;
+    std::unique_ptr<Request> r(new Request());
+    uint32_t n = 0;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (model_id >= s->models.size()) return FL_ERR_MODEL_NOT_SET;
+        n = s->models[model_id]->n;
+        if (s->budget < footprint(*s->models[model_id]) && s->models[model_id]->idle.empty()) {
+            fl::set_last_error("fl_server_submit: the model does not fit the HBM budget");
+            return FL_ERR_OUT_OF_MEMORY;
+        }
+    }
+    r->model = model_id;
+    r->base.assign(base, base + n);
+    r->k.assign(erodibility, erodibility + n);
+    r->u.assign(uplift, uplift + n);
+    r->outlet.assign(is_outlet, is_outlet + n);
+    if (max_slope) {
+        r->has_slope = true;
+        r->slope.assign(max_slope, max_slope + n);
+    }
+    r->max_iter = max_iteration;
+    r->out = out_elev;
+    r->arrived = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        r->id = s->next_id++;
+        *ticket = r->id;
+        s->queue.push_back(r.get());
+        s->requests[r->id] = std::move(r);
+    }
+    s->cv_work.notify_all();
+    return FL_OK;
+}
+
+int fl_server_wait(fl_server* s, uint64_t ticket, uint32_t* out_iterations, double* latency_ms,
+                   double* queue_ms, double* solve_ms) {
+    if (!s) return FL_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->requests.find(ticket);
+    if (it == s->requests.end()) {
+        fl::set_last_error("fl_server_wait: unknown ticket");
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    Request* r = it->second.get();
+    s->cv_done.wait(lk, [&] { return r->done; });
+    if (out_iterations) *out_iterations = r->iterations;
+    if (latency_ms) *latency_ms = ms_between(r->arrived, r->finished);
+    if (queue_ms) *queue_ms = ms_between(r->arrived, r->started);
+    if (solve_ms) *solve_ms = ms_between(r->started, r->finished);
+    const int rc = r->status;
+    if (rc != FL_OK) fl::set_last_error(r->error.c_str());
+    s->requests.erase(it);
+    return rc;
+}
+
+int fl_server_stats(fl_server* s, uint64_t* out, uint32_t cap) {
+    if (!s || !out) return FL_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    const uint64_t v[] = {s->completed, s->peak_active, s->peak_used, s->used, s->created,
+                          s->evicted, (uint64_t)s->queue.size()};
+    for (uint32_t i = 0; i < cap && i < sizeof v / sizeof v[0]; ++i) out[i] = v[i];
+    return FL_OK;
+}
+
+void fl_server_destroy(fl_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    for (auto& t : s->workers) t.join();
+    for (auto& m : s->models)
+        for (fl_graph* g : m->idle) fl_graph_destroy(g);
+    delete s;
+}
+
+}  // extern "C"

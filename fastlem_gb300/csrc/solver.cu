@@ -243,6 +243,7 @@ struct fl_graph {
     uint32_t n = 0;
     uint64_t nnz = 0;
     int device = 0;
+    uint64_t dev_bytes = 0;   // device memory the model holds
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // host copies used by the host-side lake-heap rank
@@ -311,9 +312,14 @@ struct fl_graph {
 
 namespace {
 
+// Device bytes allocated on this thread are added here while a model is being created.
+thread_local uint64_t* t_alloc_bytes = nullptr;
+
 template <class T>
 int dalloc(T** p, uint64_t count) {
-    FL_CU(cudaMalloc((void**)p, std::max<uint64_t>(1, count) * sizeof(T)));
+    const uint64_t bytes = std::max<uint64_t>(1, count) * sizeof(T);
+    FL_CU(cudaMalloc((void**)p, bytes));
+    if (t_alloc_bytes) *t_alloc_bytes += bytes;
     return FL_OK;
 }
 
@@ -457,9 +463,12 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_bu_done, n));
     FL_TRY(dalloc(&g->d_td_need, n));
     FL_TRY(dalloc(&g->d_td_done, n));
+    // stamp-tagged words start below every stamp (stamps count from 1 per model, and
+    // the memory may have belonged to an earlier model)
     FL_CU(cudaMemset(g->d_bu_done, 0, n * 4ull));
     FL_CU(cudaMemset(g->d_td_need, 0, n * 4ull));
     FL_CU(cudaMemset(g->d_td_done, 0, n * 4ull));
+    FL_CU(cudaMemset(g->d_push, 0, n * 8ull));
     FL_CU(cudaMemset(g->d_flags, 0, kNumFlags * 4ull));
     return FL_OK;
 }
@@ -674,6 +683,7 @@ int run_basin_pass(fl_graph* g, int* changed) {
         FL_CU(cudaMemsetAsync(g->d_bu_done, 0, g->n * 4ull, g->stream));
         FL_CU(cudaMemsetAsync(g->d_td_need, 0, g->n * 4ull, g->stream));
         FL_CU(cudaMemsetAsync(g->d_td_done, 0, g->n * 4ull, g->stream));
+        FL_CU(cudaMemsetAsync(g->d_push, 0, g->n * 8ull, g->stream));
     }
     fl::BasinArgs a{};
     a.n = g->n;
@@ -926,6 +936,10 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
     g->n = n;
     g->nnz = nnz;
     g->terrains = k_terr;
+    struct Track {
+        explicit Track(uint64_t* b) { t_alloc_bytes = b; }
+        ~Track() { t_alloc_bytes = nullptr; }
+    } track(&g->dev_bytes);
     g->site_off = so;
     g->def_off = dof;
     g->perm.resize(n);
@@ -1014,6 +1028,8 @@ int fl_batch_create(uint32_t terrains, const uint32_t* site_off, const uint32_t*
 }
 
 uint32_t fl_graph_num_terrains(const fl_graph* g) { return g ? g->terrains : 0; }
+
+uint64_t fl_graph_device_bytes(const fl_graph* g) { return g ? g->dev_bytes : 0; }
 
 int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
                       const double* erodibility, const double* uplift, const uint8_t* is_outlet,

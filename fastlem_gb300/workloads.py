@@ -160,3 +160,36 @@ def batched(count=512, lo=4096, hi=262144, seed=3, threads=None):
                          {"terrains": count, "sites": int(ns.sum()), "n_range": [lo, hi],
                           "seed": seed, "outlets": "border<2% of side",
                           "erodibility": "lognormal(0,0.5)"})
+
+
+
+@dataclass
+class ServedWorkload:
+    name: str
+    models: list
+    params: list
+    arrivals: np.ndarray          # seconds after the first request
+    config: dict = field(default_factory=dict)
+
+
+def served(count=64, rate=200.0, lo=16384, hi=4194304, seed=5, threads=None):
+    """A Poisson stream of generate() requests at `rate` per second (seed 5), site counts
+    log-uniform in [16384, 4194304], each terrain uniform-random in its own square of
+    side sqrt(n) with border outlets within 2% of the side and its own seeded
+    erodibility field clamp(exp(N(0,0.5)) * (0.5 + 4-octave value noise), 0.1, 4)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, count)
+    arrivals = np.concatenate([[0.0], np.cumsum(gaps[1:])])
+    ns = np.exp(rng.uniform(math.log(lo), math.log(hi), count)).astype(np.int64)
+    seeds = rng.integers(1, 2**31, count)
+    specs = [(int(n), math.sqrt(n), int(sd)) for n, sd in zip(ns, seeds)]
+    models = _build_many(specs, threads or os.cpu_count() or 1)
+    params = []
+    for (n, side, sd), m in zip(specs, models):
+        r = np.random.default_rng(int(sd) + 1)
+        v = value_noise(m.xs, m.ys, int(sd) % 100000, wavelength=max(4.0, side / 8))
+        k = np.clip(np.exp(r.normal(0.0, 0.5, n)) * (0.5 + v), 0.1, 4.0)
+        params.append(ParameterArrays(n, erodibility=k, is_outlet=border_outlets(m, side, 0.02 * side)))
+    return ServedWorkload("served", models, params, arrivals,
+                          {"requests": count, "rate_per_s": rate, "sites": int(ns.sum()),
+                           "n_range": [lo, hi], "seed": seed})

@@ -111,6 +111,9 @@ int fl_batch_create(uint32_t terrains, const uint32_t* site_off, const uint32_t*
 /* Number of packed terrains of a model (1 for fl_graph_create models). */
 uint32_t fl_graph_num_terrains(const fl_graph* g);
 
+/* Device memory a model holds (graph and workspace), in bytes. */
+uint64_t fl_graph_device_bytes(const fl_graph* g);
+
 /* generate() for every packed terrain at once: per-site parameters over all sites, one
  * max_iteration for all.  out_terrain_iterations[t] = the loop bodies terrain t would
  * have run alone (its first iteration without an elevation change, or the limit);
@@ -121,6 +124,50 @@ int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
                       const double* max_slope, int64_t max_iteration, double* out_elev,
                       uint32_t* out_terrain_iterations, uint32_t* out_iterations,
                       double* loop_ms, double* total_ms);
+
+/* ---- served form (no fastlem counterpart: a request loop of generate() calls) ------
+ *
+ * Models are registered once (the server keeps a host copy); requests name a model
+ * and carry their own parameters.  `slots` worker threads run up to that many requests
+ * at once, each on its own CUDA stream, so their kernels overlap on the GPU.  A
+ * request needs a device instance of its model (fl_graph_device_bytes of HBM); the
+ * oldest waiting request starts once a slot is free and its model has an idle
+ * instance or a new one fits `hbm_budget_bytes` after evicting idle instances (least
+ * recently used first).  Instances stay resident for later requests on the same
+ * model.  A request's elevations equal fl_generate's for the same model and
+ * parameters.  Create and use the server on the device selected when it is created. */
+typedef struct fl_server fl_server;
+
+int fl_server_create(uint64_t hbm_budget_bytes, uint32_t slots, fl_server** out);
+
+/* Registers a model (arguments as fl_graph_create; the arrays are copied). */
+int fl_server_add_model(fl_server* s, uint32_t n, const uint32_t* row_ptr, const uint32_t* col,
+                        const double* len, const double* area, const uint32_t* default_outlets,
+                        uint32_t n_default, const double* xs, const double* ys,
+                        uint32_t* model_id);
+
+/* Queues generate() for a registered model; parameters as fl_generate (copied before
+ * return).  out_elev (n entries) is written by the time fl_server_wait returns and
+ * must stay valid until then.  FL_ERR_OUT_OF_MEMORY when the model can never fit the
+ * budget. */
+int fl_server_submit(fl_server* s, uint32_t model_id, const double* base,
+                     const double* erodibility, const double* uplift, const uint8_t* is_outlet,
+                     const double* max_slope, int64_t max_iteration, double* out_elev,
+                     uint64_t* ticket);
+
+/* Blocks until the request is done; returns its fl_generate status and, optionally,
+ * its iterations, latency (submit to done), queueing and solve times in ms.  A ticket
+ * can be waited for once. */
+int fl_server_wait(fl_server* s, uint64_t ticket, uint32_t* out_iterations, double* latency_ms,
+                   double* queue_ms, double* solve_ms);
+
+/* Up to `cap` counters: requests completed, peak concurrent requests, peak and current
+ * device bytes of instances, instances created, instances evicted, requests waiting. */
+int fl_server_stats(fl_server* s, uint64_t* out, uint32_t cap);
+
+/* Stops the workers after the requests they are running; waiting requests are
+ * dropped.  Frees every instance. */
+void fl_server_destroy(fl_server* s);
 
 /* Message for the last error on this thread ("" when none). */
 const char* fl_last_error(void);

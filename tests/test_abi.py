@@ -95,3 +95,35 @@ def test_batch_create_rejects_edges_across_terrains(fl_lib):
                                 ptr(length), ptr(area), ptr(def_off), ptr(defs), None, None,
                                 ctypes.byref(h))
     assert rc == FL_ERR_INVALID_ARGUMENT
+
+
+def test_server_host_checks(fl_lib):
+    """Server argument checks that run before any device work."""
+    import ctypes
+    import numpy as np
+    from fastlem_gb300._lib import (FL_ERR_INVALID_ARGUMENT, FL_ERR_MODEL_NOT_SET,
+                                    FL_ERR_OUT_OF_MEMORY, ptr)
+    s = ctypes.c_void_p()
+    assert fl_lib.fl_server_create(0, 2, ctypes.byref(s)) == FL_ERR_INVALID_ARGUMENT
+    assert fl_lib.fl_server_create(1 << 20, 1, ctypes.byref(s)) == 0
+    try:
+        row_ptr = np.array([0, 1, 2], np.uint32)
+        col = np.array([1, 0], np.uint32)
+        length = np.ones(2)
+        area = np.ones(2)
+        defs = np.array([0], np.uint32)
+        mid = ctypes.c_uint32()
+        assert fl_lib.fl_server_add_model(s, 2, ptr(row_ptr), ptr(col), ptr(length), ptr(area),
+                                          ptr(defs), 1, None, None, ctypes.byref(mid)) == 0
+        z, o = np.zeros(2), np.ones(2)
+        out = np.empty(2)
+        t = ctypes.c_uint64()
+        outl = np.zeros(2, np.uint8)
+        # unknown model, then a model whose instance can never fit a 1 MiB budget
+        assert fl_lib.fl_server_submit(s, 7, ptr(z), ptr(o), ptr(o), ptr(outl), None, -1,
+                                       ptr(out), ctypes.byref(t)) == FL_ERR_MODEL_NOT_SET
+        assert fl_lib.fl_server_submit(s, mid.value, ptr(z), ptr(o), ptr(o), ptr(outl), None, -1,
+                                       ptr(out), ctypes.byref(t)) == FL_ERR_OUT_OF_MEMORY
+        assert fl_lib.fl_server_wait(s, 12345, None, None, None, None) == FL_ERR_INVALID_ARGUMENT
+    finally:
+        fl_lib.fl_server_destroy(s)
