@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--iters", type=int, default=8, help="set_max_iteration per step")
     ap.add_argument("--cpu-iters", type=int, default=1, help="iterations in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="16M run: skip the batched (C4) and served (C5) summaries")
     return ap.parse_args()
 
 
@@ -148,6 +150,29 @@ def peak_hbm():
         with open(p) as f:
             return float(json.load(f)["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+# DRAM bytes (read + write) of one launch from an ncu capture, per unit the kernel
+# processes; a capture of the full 16M workload does not fit the profiling size rule,
+# so the 1M config's launch is scaled by the units (traffic grows with them).
+NCU_TRAFFIC = {
+    # profiles/k_kahn_1m.md: 52.80 MB for the 921,868 Kahn-region sites of the 1M config
+    "kahn_rounds": (52.80e6 / 921_868, "kahn_sites",
+                    "ncu dram__bytes_read+write of one k_kahn launch on the 1M config "
+                    "(profiles/k_kahn_1m.md), scaled by Kahn-region sites"),
+    # profiles/k_s_bottom_up_1m.md: 4.31 MB for 78,132 skeleton sites
+    "skeleton_up": (4.31e6 / 78_132, "skeleton_sites",
+                    "ncu dram__bytes_read+write of one k_s_bottom_up launch on the 1M config "
+                    "(profiles/k_s_bottom_up_1m.md), scaled by skeleton sites"),
+}
+
+
+def measured_traffic(kernel, basin, n):
+    if kernel not in NCU_TRAFFIC:
+        return None, "no ncu capture for this kernel"
+    per, unit, src = NCU_TRAFFIC[kernel]
+    units = basin["skeleton_sites"] if unit == "skeleton_sites" else n - basin["skeleton_sites"]
+    return per * units, src
 
 
 def make_workload(args):
@@ -255,8 +280,10 @@ def bench_gpu(args, d):
     achieved = (dbytes / dl) / ((dms / dl) / 1000) / 1e9 if dl and dms else 0.0
     all_bytes = sum(v[2] for v in stats.values())
     all_ms = sum(v[1] for v in stats.values())
+    traffic, traffic_src = measured_traffic(dname, basin, n)
     roof = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "traffic_source": traffic_src,
             "bytes_per_launch": dbytes / max(1, dl), "ms_per_launch": dms / max(1, dl),
             "launches": dl,
             # every kernel class together: algorithmic bytes of the whole solve over its
@@ -296,10 +323,24 @@ def bench_gpu(args, d):
         "clocks": clocks.summary(),
         "wall_ms_timed": wall_ms,
     }
+    if not args.no_extras and args.gpus == 1 and args.config == "16m":
+        # the other two parts of the headline metric, on the same GPU after the 16M run
+        import copy
+        ea = copy.copy(args)
+        ea.steps, ea.warmup, ea.batch_iters, ea.requests, ea.serve_iters = 2, 1, 64, 32, 64
+        b = bench_batched(ea, d, emit=False)
+        line["batched"] = {k: b[k] for k in ("metric", "value", "unit", "e2e", "plain_loop",
+                                              "speedup_vs_plain_loop", "identical_to_plain")}
+        line["batched"]["config"] = b["config"]
+        sv = bench_served(ea, d, emit=False)
+        line["served"] = {k: sv[k] for k in ("metric", "value", "unit", "latency_ms",
+                                              "sequential_plain", "speedup_vs_sequential",
+                                              "identical_to_plain", "server")}
+        line["served"]["config"] = sv["config"]
     print(json.dumps(line), flush=True)
 
 
-def bench_batched(args, d):
+def bench_batched(args, d, emit=True):
     """C4: 512 terrains of uneven size solved as one packed graph, against the plain
     per-terrain loop (one TerrainGenerator.generate() after another) on the same GPU.
     A step solves every terrain to convergence (generator defaults)."""
@@ -381,10 +422,12 @@ def bench_batched(args, d):
         "identical_to_plain": identical,
         "clocks": clocks.summary(),
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
-def bench_served(args, d):
+def bench_served(args, d, emit=True):
     """C5: a Poisson stream of generate() requests (200 req/s, 16,384-4,194,304 sites)
     replayed in real time, once through the server (concurrent requests, resident
     models, 120 GB HBM admission budget) and once one request at a time through the
@@ -463,7 +506,9 @@ def bench_served(args, d):
         "server": stats,
         "clocks": clocks.summary(),
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
