@@ -31,6 +31,7 @@ EXPORTS = [
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
     "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate", "fl_graph_device_bytes",
+    "fl_model_device_bytes",
     "fl_server_create", "fl_server_add_model", "fl_server_submit", "fl_server_wait",
     "fl_server_stats", "fl_server_destroy",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
@@ -67,6 +68,8 @@ def lib():
     L.fl_graph_num_terrains.restype = c_u32
     L.fl_graph_device_bytes.argtypes = [vp]
     L.fl_graph_device_bytes.restype = c_u64
+    L.fl_model_device_bytes.argtypes = [c_u32, c_u64]
+    L.fl_model_device_bytes.restype = c_u64
     L.fl_server_create.argtypes = [c_u64, c_u32, P(vp)]
     L.fl_server_add_model.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, c_u32, vp, vp, P(c_u32)]
     L.fl_server_submit.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, ctypes.c_int64, vp, P(c_u64)]

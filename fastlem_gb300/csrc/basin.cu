@@ -261,22 +261,23 @@ __global__ void k_s_rank(uint32_t* ptr0, uint32_t* dist0, uint32_t* ptr1, uint32
 }
 
 // Chain ids for chain bottoms.
+// Chain ids for the chain bottoms (skeleton sites that point at themselves after the
+// ranking), in skeleton order, one reservation per block.
 __global__ void k_s_bottoms(const uint32_t* __restrict__ slist, Ranks rk,
                             uint32_t* __restrict__ cid, uint32_t* __restrict__ cbot,
                             uint32_t max_chains, uint32_t* meta, int* flags) {
-    uint32_t ns = meta[kMetaNs];
+    const uint32_t ns = meta[kMetaNs];
     const uint32_t* ptr = rk.P(meta);
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
-        if (ptr[k] == k) {
-            uint32_t c = atomicAdd(&meta[kMetaChains], 1u);
+    block_range_compact(
+        ns, &meta[kMetaChains], [&](uint32_t k) { return ptr[k] == k; },
+        [&](uint32_t k, uint32_t c) {
             if (c < max_chains) {
                 cid[k] = c;
                 cbot[c] = slist[k];
             } else {
                 set_error(flags, kErrCapacity);
             }
-        }
-    }
+        });
 }
 
 // Chain lengths from the skeleton leaves (the final Kahn frontier).
@@ -287,11 +288,17 @@ __global__ void k_s_lengths(const uint32_t* __restrict__ order, const uint32_t* 
     uint32_t b = meta[kMetaFrontBeg], e = meta[kMetaFrontEnd];
     const uint32_t* ptr = rk.P(meta);
     const uint32_t* dist = rk.D(meta);
-    for (uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
-        uint32_t k = sid[order[i]];
-        uint32_t c = cid[ptr[k]];
-        if (c < max_chains) clen[c] = dist[k] + 1;
-        atomicMax(&meta[kMetaMaxChain], dist[k] + 1);
+    for (uint32_t base = b + blockIdx.x * blockDim.x; base < e; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t l = 0;
+        if (i < e) {
+            uint32_t k = sid[order[i]];
+            uint32_t c = cid[ptr[k]];
+            l = dist[k] + 1;
+            if (c < max_chains) clen[c] = l;
+        }
+        l = __reduce_max_sync(0xffffffffu, l);      // one atomic per warp
+        if ((threadIdx.x & 31) == 0 && l) atomicMax(&meta[kMetaMaxChain], l);
     }
 }
 
@@ -338,6 +345,108 @@ __global__ void k_s_layout(const uint32_t* __restrict__ slist, Ranks rk,
         } else {
             set_error(flags, kErrForest);
         }
+    }
+}
+
+// Lanes of the warp holding the same key: one atomicAdd per distinct key; returns
+// the lane's slot (old value + its rank among the lanes with that key).
+__device__ __forceinline__ uint32_t grouped_add(uint32_t* base, uint32_t key, bool active) {
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!active) return 0;
+    const unsigned peers = __match_any_sync(act, key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    uint32_t b = 0;
+    if (lane == leader) b = atomicAdd(&base[key], (uint32_t)__popc(peers));
+    b = __shfl_sync(peers, b, leader);
+    return b + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// The chain tree (cooperative).  A chain's parent is the chain holding the site its
+// bottom drains to (itself for a chain that ends at a root).  Pointer jumping gives every
+// chain its root chain (cpar) and depth; a counting sort by depth gives corder, the
+// shallowest chains first.  A chain only ever waits for its children (bottom-up: the
+// chains ending on it) or its parent (top-down), so walkers that claim chains deepest
+// first (bottom-up) or shallowest first (top-down) never wait for an unclaimed chain.
+__global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t* __restrict__ layout,
+                               const uint32_t* __restrict__ coff, const uint32_t* __restrict__ sid,
+                               const uint32_t* __restrict__ kslot,
+                               const uint32_t* __restrict__ slot_chain, uint32_t* par0,
+                               uint32_t* dep0, uint32_t* par1, uint32_t* dep1,
+                               uint32_t* __restrict__ cqp, uint32_t* cpar, uint32_t* hist,
+                               uint32_t* __restrict__ corder, uint32_t* meta, int* flags) {
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    if (ld_acquire(&flags[kError])) return;
+    const uint32_t nc = meta[kMetaChains];
+    for (uint32_t c = gtid; c < nc; c += stride) {
+        const uint32_t v = layout[coff[c]];
+        const uint32_t p = next[v];
+        hist[c] = 0;
+        if (p == v) {
+            par0[c] = c;
+            dep0[c] = 0;
+            cqp[c] = kNone;
+        } else {
+            const uint32_t q = kslot[sid[p]];
+            cqp[c] = q;
+            par0[c] = slot_chain[q];
+            dep0[c] = 1;
+        }
+    }
+    if (!grid_barrier(flags)) return;
+    // ceil(log2(nc)) + 1 rounds reach every root (depths are below nc)
+    int rounds = 1;
+    while ((1u << (rounds - 1)) < nc && rounds < 32) ++rounds;
+    uint32_t *pin = par0, *din = dep0, *pout = par1, *dout = dep1;
+    for (int r = 0; r < rounds; ++r) {
+        for (uint32_t c = gtid; c < nc; c += stride) {
+            const uint32_t p = pin[c];
+            pout[c] = pin[p];
+            dout[c] = p == c ? din[c] : din[c] + din[p];
+        }
+        if (!grid_barrier(flags)) return;
+        uint32_t* t = pin; pin = pout; pout = t;
+        t = din; din = dout; dout = t;
+    }
+    for (uint32_t base = blockIdx.x * blockDim.x; base < nc; base += stride) {
+        const uint32_t c = base + threadIdx.x;
+        const bool act = c < nc;
+        const uint32_t d = act ? din[c] : 0;
+        if (act) {
+            cpar[c] = pin[c];
+            if (d >= nc || pin[pin[c]] != pin[c]) set_error(flags, kErrForest);
+        }
+        grouped_add(hist, act ? d : 0, act);
+    }
+    if (!grid_barrier(flags)) return;
+    if (blockIdx.x == 0) {                       // exclusive scan of the depth counts
+        __shared__ uint32_t part[1024];
+        const uint32_t per = (nc + blockDim.x - 1) / blockDim.x;
+        const uint32_t b = threadIdx.x * per, e = min(nc, b + per);
+        uint32_t sum = 0;
+        for (uint32_t i = b; i < e; ++i) sum += hist[i];
+        part[threadIdx.x] = sum;
+        __syncthreads();
+        for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+            const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+            __syncthreads();
+            part[threadIdx.x] += v;
+            __syncthreads();
+        }
+        uint32_t run = part[threadIdx.x] - sum;
+        for (uint32_t i = b; i < e; ++i) {
+            const uint32_t h = hist[i];
+            hist[i] = run;
+            run += h;
+        }
+    }
+    if (!grid_barrier(flags)) return;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < nc; base += stride) {
+        const uint32_t c = base + threadIdx.x;
+        const bool act = c < nc;
+        const uint32_t pos = grouped_add(hist, act ? din[c] : 0, act);
+        if (act) corder[pos] = c;
     }
 }
 
@@ -595,111 +704,121 @@ k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col
               const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
               const SlotRec* __restrict__ rec, const SlotInfo* __restrict__ info,
               double* tokval, const uint64_t* __restrict__ push_to, double* __restrict__ Al,
-              int* bu_done, int stamp, uint32_t* meta, int* flags) {
+              const uint32_t* __restrict__ corder, int* bu_done, int stamp, uint32_t* meta,
+              int* flags) {
     constexpr int S = kUpSlots;
     __shared__ SlotRec s_rec[kWalkWarps][kStages][32 * S];
     __shared__ SlotInfo s_info[kWalkWarps][kStages][32 * S];
     const int lane = threadIdx.x & 31;
     const int wb = threadIdx.x >> 5;
-    const uint32_t c = blockIdx.x * kWalkWarps + wb;
-    // warp-uniform exits only: the warp shuffles with the full mask below
-    if (c >= meta[kMetaChains] || __any_sync(kFull, ld_acquire(&flags[kError]) != 0)) return;
-    const uint32_t off = coff[c];
-    const uint32_t len = clen[c];
-    if (off + len > meta[kMetaNs] || len == 0) {
-        if (lane == 0) set_error(flags, kErrForest);
-        return;
-    }
-    const uint64_t t_start = global_ns();
-    uint32_t slow_cycles = 0, slow_n = 0;
-    // round r, lane l, slot s is the slot (32 r + l) S + s places below the chain's leaf
-    const uint32_t per_round = 32 * S;
-    const uint32_t nrounds = (len + per_round - 1) / per_round;
-    const uint32_t top = off + len - 1;
-    auto issue = [&](uint32_t r) {                   // one commit group per round
-        if (r < nrounds) {
-#pragma unroll
-            for (int sl = 0; sl < S; ++sl) {
-                const uint32_t back = r * per_round + lane * S + sl;
-                if (back < len) {
-                    const uint32_t q = top - back;
-                    SlotRec* dst = &s_rec[wb][r % kStages][lane * S + sl];
-                    cp_async16(&dst->pre, &rec[q].pre);
-                    cp_async16(&dst->p1, &rec[q].p1);
-                    cp_async8(&s_info[wb][r % kStages][lane * S + sl], &info[q]);
+    const uint32_t nc = meta[kMetaChains];
+    // persistent warps claim chains deepest first (a chain waits only for the chains
+    // ending on it, which are deeper); warp-uniform exits only
+    while (true) {
+        if (__any_sync(kFull, ld_acquire(&flags[kError]) != 0)) return;
+        uint32_t idx = 0;
+        if (lane == 0) idx = atomicAdd(&meta[kMetaClaimUp], 1u);
+        idx = __shfl_sync(kFull, idx, 0);
+        if (idx >= nc) return;
+        const uint32_t c = corder[nc - 1 - idx];
+        const uint32_t off = coff[c];
+        const uint32_t len = clen[c];
+        if (off + len > meta[kMetaNs] || len == 0) {
+            if (lane == 0) set_error(flags, kErrForest);
+            return;
+        }
+        const uint64_t t_start = global_ns();
+        uint32_t slow_cycles = 0, slow_n = 0;
+        // round r, lane l, slot s is the slot (32 r + l) S + s places below the chain's leaf
+        const uint32_t per_round = 32 * S;
+        const uint32_t nrounds = (len + per_round - 1) / per_round;
+        const uint32_t top = off + len - 1;
+        auto issue = [&](uint32_t r) {                   // one commit group per round
+            if (r < nrounds) {
+    #pragma unroll
+                for (int sl = 0; sl < S; ++sl) {
+                    const uint32_t back = r * per_round + lane * S + sl;
+                    if (back < len) {
+                        const uint32_t q = top - back;
+                        SlotRec* dst = &s_rec[wb][r % kStages][lane * S + sl];
+                        cp_async16(&dst->pre, &rec[q].pre);
+                        cp_async16(&dst->p1, &rec[q].p1);
+                        cp_async8(&s_info[wb][r % kStages][lane * S + sl], &info[q]);
+                    }
                 }
             }
-        }
-        cp_async_commit();
-    };
-#pragma unroll
-    for (int r = 0; r < kStages - 1; ++r) issue(r);
-    double x = 0.0;
-    bool ok = true;
-    uint32_t spins = 0;
-    for (uint32_t r = 0; r < nrounds; ++r) {
-        __syncwarp();                                // stage r - 1 is no longer read
-        issue(r + kStages - 1);
-        cp_async_wait<kStages - 1>();                // this round's copies have landed
-        __syncwarp();                                // ... for every lane
-        const int st = r % kStages;
-        const uint32_t left = len - r * per_round;
-        const int cnt = left < per_round ? (int)((left + S - 1) / S) : 32;
-        const int nsl = (uint32_t)lane * S < left ? (int)min((uint32_t)S, left - lane * S) : 0;
-        uint32_t nopm = 0, specm = 0;
-#pragma unroll
-        for (int sl = 0; sl < S; ++sl) {
-            if (sl < nsl) {
-                const uint32_t fl = s_info[wb][st][lane * S + sl].flags;
-                nopm |= ((fl >> kPostShift) & 3u) << (2 * sl);
-                if (fl & (kLeafSlot | kTok | kSlow)) specm |= 1u << sl;
-            }
-        }
-        auto opnd = [&](int l, int sl, int j) -> double {
-            return reinterpret_cast<const double*>(&s_rec[wb][st][l * S + sl])[j];
+            cp_async_commit();
         };
-        x = warp_fold_slots<S, 4>(
-            x, cnt, nsl, nopm, specm, [&](int sl, int j) { return opnd(lane, sl, j); },
-            [&](int l, int sl, int j) { return opnd(l, sl, j); },
-            [&](int l, int sl, double xin) -> double {
-                const SlotInfo si = s_info[wb][st][l * S + sl];
-                const uint32_t q = top - (r * per_round + l * S + sl);
-                if (!ok) return xin;
-                const long long c0 = clock64();
-                double res;
-                if (si.flags & kTok) {
-                    res = warp_list_pull(tokval, si.tokoff, (si.flags >> kTokCntShift) & 15u,
-                                         (si.flags >> kHeavyShift) & 15u, xin, flags, &ok, &spins);
-                } else if (si.flags & kSlow) {
-                    res = warp_slow_pull(layout[q], (si.flags & kLeafSlot) ? kNone : layout[q + 1],
-                                         xin, row, col, next, hgt, area, A, bu_done, stamp, flags,
-                                         &ok, &spins);
-                } else {
-                    return opnd(l, sl, 0);             // chain leaf: its own complete pull
+    #pragma unroll
+        for (int r = 0; r < kStages - 1; ++r) issue(r);
+        double x = 0.0;
+        bool ok = true;
+        uint32_t spins = 0;
+        for (uint32_t r = 0; r < nrounds; ++r) {
+            __syncwarp();                                // stage r - 1 is no longer read
+            issue(r + kStages - 1);
+            cp_async_wait<kStages - 1>();                // this round's copies have landed
+            __syncwarp();                                // ... for every lane
+            const int st = r % kStages;
+            const uint32_t left = len - r * per_round;
+            const int cnt = left < per_round ? (int)((left + S - 1) / S) : 32;
+            const int nsl = (uint32_t)lane * S < left ? (int)min((uint32_t)S, left - lane * S) : 0;
+            uint32_t nopm = 0, specm = 0;
+    #pragma unroll
+            for (int sl = 0; sl < S; ++sl) {
+                if (sl < nsl) {
+                    const uint32_t fl = s_info[wb][st][lane * S + sl].flags;
+                    nopm |= ((fl >> kPostShift) & 3u) << (2 * sl);
+                    if (fl & (kLeafSlot | kTok | kSlow)) specm |= 1u << sl;
                 }
-                slow_cycles += (uint32_t)(clock64() - c0);
-                ++slow_n;
-                return res;
-            },
-            [&](int sl, double v) { Al[top - (r * per_round + lane * S + sl)] = v; });
-        if (!ok) break;
-    }
-    cp_async_wait<0>();                              // nothing in flight at exit
-    if (!ok) return;
-    if (lane == 0) {
-        uint32_t bottom = layout[off];
-        A[bottom] = x;
-        st_release(&bu_done[bottom], stamp);          // orders the store above
-        const uint64_t pt = push_to[bottom];
-        if ((uint32_t)(pt >> 32) == (uint32_t)stamp) {
-            uint64_t xb = (uint64_t)__double_as_longlong(x);
-            if (isnan(x)) xb = 0x7ff8000000000000ull;   // never the pending marker
-            st_relaxed_u64(&tokval[(uint32_t)pt], xb);
+            }
+            auto opnd = [&](int l, int sl, int j) -> double {
+                return reinterpret_cast<const double*>(&s_rec[wb][st][l * S + sl])[j];
+            };
+            x = warp_fold_slots<S, 4>(
+                x, cnt, nsl, nopm, specm, [&](int sl, int j) { return opnd(lane, sl, j); },
+                [&](int l, int sl, int j) { return opnd(l, sl, j); },
+                [&](int l, int sl, double xin) -> double {
+                    const SlotInfo si = s_info[wb][st][l * S + sl];
+                    const uint32_t q = top - (r * per_round + l * S + sl);
+                    if (!ok) return xin;
+                    const long long c0 = clock64();
+                    double res;
+                    if (si.flags & kTok) {
+                        res = warp_list_pull(tokval, si.tokoff, (si.flags >> kTokCntShift) & 15u,
+                                             (si.flags >> kHeavyShift) & 15u, xin, flags, &ok, &spins);
+                    } else if (si.flags & kSlow) {
+                        res = warp_slow_pull(layout[q], (si.flags & kLeafSlot) ? kNone : layout[q + 1],
+                                             xin, row, col, next, hgt, area, A, bu_done, stamp, flags,
+                                             &ok, &spins);
+                    } else {
+                        return opnd(l, sl, 0);             // chain leaf: its own complete pull
+                    }
+                    slow_cycles += (uint32_t)(clock64() - c0);
+                    ++slow_n;
+                    return res;
+                },
+                [&](int sl, double v) { Al[top - (r * per_round + lane * S + sl)] = v; });
+            if (!ok) break;
         }
+        cp_async_wait<0>();                              // nothing in flight at exit
+        if (!ok) return;
+        if (lane == 0) {
+            uint32_t bottom = layout[off];
+            A[bottom] = x;
+            st_release(&bu_done[bottom], stamp);          // orders the store above
+            const uint64_t pt = push_to[bottom];
+            if ((uint32_t)(pt >> 32) == (uint32_t)stamp) {
+                uint64_t xb = (uint64_t)__double_as_longlong(x);
+                if (isnan(x)) xb = 0x7ff8000000000000ull;   // never the pending marker
+                st_relaxed_u64(&tokval[(uint32_t)pt], xb);
+            }
+        }
+        spins = __reduce_add_sync(kFull, spins);
+        if (lane == 0 && spins) atomicAdd(&meta[kMetaSpinUp], spins);
+        if (lane == 0)
+            record_chain_stat(meta, kMetaUpSlow, global_ns() - t_start, slow_cycles, slow_n);
     }
-    spins = __reduce_add_sync(kFull, spins);
-    if (lane == 0 && spins) atomicAdd(&meta[kMetaSpinUp], spins);
-    if (lane == 0) record_chain_stat(meta, kMetaUpSlow, global_ns() - t_start, slow_cycles, slow_n);
 }
 
 // Skeleton areas back to site order.
@@ -816,66 +935,41 @@ __device__ __forceinline__ double settle(const TopDown& td, uint32_t v, uint32_t
                       __ldcg(&td.elev[v]), td.outlet[v] != 0, e_out, changed);
 }
 
-// Per chain, before the top-down walk (one block): the layout slot of the site it
-// hangs from (kNone for a chain that starts at a root), and its basin outlet with the
-// outlet's response time and elevation, inherited from the chain tree's root chain by
-// pointer jumping.  Root sites are settled here (t = 0 + (0 + w), elevation with the
-// outlet's own update), and their response time / elevation stored in the layout
-// arrays and published for the slope-limited walk.
-__global__ void k_s_chain_roots(TopDown td, const uint32_t* __restrict__ layout,
-                                const uint32_t* __restrict__ coff,
-                                const uint32_t* __restrict__ sid,
-                                const uint32_t* __restrict__ kslot,
-                                const uint32_t* __restrict__ slot_chain, uint32_t* cpar,
-                                uint32_t* __restrict__ cqp, uint32_t* __restrict__ cbas,
-                                double* __restrict__ cto, double* __restrict__ ceo,
-                                double* __restrict__ tl, double* __restrict__ el, int* td_done,
-                                int stamp, const uint32_t* meta) {
+// Before the top-down walk: root chains settle their root site (t = 0 + (0 + w), the
+// outlet's own elevation update) and store its response time / elevation in the layout
+// arrays, publishing it for the slope-limited walk; then every chain takes its basin
+// outlet and the outlet's response time and elevation from its root chain (cpar).
+__global__ void k_s_settle_roots(TopDown td, const uint32_t* __restrict__ layout,
+                                 const uint32_t* __restrict__ coff,
+                                 const uint32_t* __restrict__ cqp, uint32_t* __restrict__ cbas,
+                                 double* __restrict__ cto, double* __restrict__ ceo,
+                                 double* __restrict__ tl, double* __restrict__ el, int* td_done,
+                                 int stamp, const uint32_t* meta) {
     if (td.flags[kError]) return;
     const uint32_t nc = meta[kMetaChains];
     bool changed = false;
-    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        if (cqp[c] != kNone) continue;
         const uint32_t off = coff[c];
         const uint32_t v = layout[off];
-        const uint32_t p = td.next[v];
-        if (p == v) {
-            double e;
-            const double tv = settle(td, v, v, TRec{}, &e, &changed);
-            tl[off] = tv;
-            el[off] = e;
-            cpar[c] = c;
-            cqp[c] = kNone;
-            cbas[c] = td.outlet[v] ? v : kNone;
-            cto[c] = tv;
-            ceo[c] = e;
-            td_done[v] = stamp;
-        } else {
-            const uint32_t qp = kslot[sid[p]];
-            cqp[c] = qp;
-            cpar[c] = slot_chain[qp];
-        }
+        double e;
+        const double tv = settle(td, v, v, TRec{}, &e, &changed);
+        tl[off] = tv;
+        el[off] = e;
+        cbas[c] = td.outlet[v] ? v : kNone;
+        cto[c] = tv;
+        ceo[c] = e;
+        td_done[v] = stamp;
     }
-    __syncthreads();
-    // root chain of every chain; values only ever move to ancestors, so the in-place
-    // update needs no second buffer
-    bool moved = true;
-    for (int round = 0; round < 40 && moved; ++round) {
-        bool any = false;
-        for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
-            const uint32_t r = cpar[c];
-            const uint32_t rr = cpar[r];
-            if (rr != r) {
-                cpar[c] = rr;
-                any = true;
-            }
-        }
-        moved = __syncthreads_or(any) != 0;
-    }
-    if (moved) {
-        if (threadIdx.x == 0) set_error(td.flags, kErrForest);
-        return;
-    }
-    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) {
+    block_flag(td.flags, kChanged, changed);
+}
+
+__global__ void k_s_root_values(const uint32_t* __restrict__ cpar, uint32_t* __restrict__ cbas,
+                                double* __restrict__ cto, double* __restrict__ ceo,
+                                const uint32_t* meta, const int* flags) {
+    if (flags[kError]) return;
+    const uint32_t nc = meta[kMetaChains];
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         const uint32_t r = cpar[c];
         if (r != c) {
             cbas[c] = cbas[r];
@@ -883,7 +977,6 @@ __global__ void k_s_chain_roots(TopDown td, const uint32_t* __restrict__ layout,
             ceo[c] = ceo[r];
         }
     }
-    block_flag(td.flags, kChanged, changed);
 }
 
 // One warp per chain, bottom to leaf: t_v = 0 + (t_parent + w_v) (below a root t is
@@ -894,80 +987,89 @@ __global__ void k_s_chain_roots(TopDown td, const uint32_t* __restrict__ layout,
 __global__ void __launch_bounds__(kWalkWarps * 32, 8)
 k_s_top_down(const int* flags, const uint32_t* __restrict__ coff,
              const uint32_t* __restrict__ clen, const uint32_t* __restrict__ cqp,
-             const double* __restrict__ wl, double* tl, uint32_t* meta) {
+             const double* __restrict__ wl, double* tl, const uint32_t* __restrict__ corder,
+             uint32_t* meta) {
+    __shared__ double s_w[kWalkWarps][kStagesDown][32 * kDownSlots];
     const int lane = threadIdx.x & 31;
     const int wb = threadIdx.x >> 5;
-    const uint32_t c = blockIdx.x * kWalkWarps + wb;
-    // warp-uniform exits only: the warp shuffles with the full mask below
-    if (c >= meta[kMetaChains] || __any_sync(kFull, ld_acquire(&flags[kError]) != 0)) return;
-    const uint32_t off = coff[c], len = clen[c];
-    if (off + len > meta[kMetaNs] || len == 0) {
-        if (lane == 0) set_error(const_cast<int*>(flags), kErrForest);
-        return;
-    }
-    const uint32_t end = off + len;
-    const uint32_t qp = cqp[c];
-    uint32_t q = off;
-    uint64_t tb = 0;
-    bool failed = false;
-    if (qp == kNone) {                   // the root was settled before the walk
-        tb = (uint64_t)__double_as_longlong(tl[off]);
-        q = off + 1;
-    } else if (lane == 0) {
-        uint32_t spins = 0;
-        const uint64_t t0 = global_ns();
-        const long long c0 = clock64();
-        tb = ld_relaxed_u64(&tl[qp]);
-        while (tb == kPendingBits) {
-            if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&flags[kError]))) {
-                set_error(const_cast<int*>(flags), kErrWait);
-                failed = true;
-                break;
-            }
-            __nanosleep(32);
+    const uint32_t nc = meta[kMetaChains];
+    // persistent warps claim chains shallowest first (a chain waits only for its
+    // parent); warp-uniform exits only
+    while (true) {
+        if (__any_sync(kFull, ld_acquire(&flags[kError]) != 0)) return;
+        uint32_t idx = 0;
+        if (lane == 0) idx = atomicAdd(&meta[kMetaClaimDown], 1u);
+        idx = __shfl_sync(kFull, idx, 0);
+        if (idx >= nc) return;
+        const uint32_t c = corder[idx];
+        const uint32_t off = coff[c], len = clen[c];
+        if (off + len > meta[kMetaNs] || len == 0) {
+            if (lane == 0) set_error(const_cast<int*>(flags), kErrForest);
+            return;
+        }
+        const uint32_t end = off + len;
+        const uint32_t qp = cqp[c];
+        uint32_t q = off;
+        uint64_t tb = 0;
+        bool failed = false;
+        if (qp == kNone) {                   // the root was settled before the walk
+            tb = (uint64_t)__double_as_longlong(tl[off]);
+            q = off + 1;
+        } else if (lane == 0) {
+            uint32_t spins = 0;
+            const uint64_t t0 = global_ns();
+            const long long c0 = clock64();
             tb = ld_relaxed_u64(&tl[qp]);
-        }
-        // the chain that waited longest for its parent
-        record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
-        if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
-    }
-    if (__shfl_sync(kFull, failed, 0)) return;
-    double tp = __longlong_as_double((long long)__shfl_sync(kFull, (unsigned long long)tb, 0));
-    constexpr int S = kDownSlots;
-    constexpr uint32_t per_round = 32 * S;
-    __shared__ double s_w[kWalkWarps][kStagesDown][32 * S];
-    const uint32_t nrounds = (end - q + per_round - 1) / per_round;
-    auto issue = [&](uint32_t r) {                   // one commit group per round
-        if (r < nrounds) {
-#pragma unroll
-            for (int sl = 0; sl < S; ++sl) {
-                const uint32_t qq = q + r * per_round + lane * S + sl;
-                if (qq < end) cp_async8(&s_w[wb][r % kStagesDown][lane * S + sl], &wl[qq]);
+            while (tb == kPendingBits) {
+                if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&flags[kError]))) {
+                    set_error(const_cast<int*>(flags), kErrWait);
+                    failed = true;
+                    break;
+                }
+                __nanosleep(32);
+                tb = ld_relaxed_u64(&tl[qp]);
             }
+            // the chain that waited longest for its parent
+            record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
+            if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
         }
-        cp_async_commit();
-    };
-#pragma unroll
-    for (int r = 0; r < kStagesDown - 1; ++r) issue(r);
-    for (uint32_t r = 0; r < nrounds; ++r) {
-        __syncwarp();                                // stage r - 1 is no longer read
-        issue(r + kStagesDown - 1);
-        cp_async_wait<kStagesDown - 1>();
-        __syncwarp();
-        const int st = r % kStagesDown;
-        const uint32_t q0 = q + r * per_round;
-        const uint32_t left = end - q0;
-        const int cnt = left < per_round ? (int)((left + S - 1) / S) : 32;
-        const int nsl = (uint32_t)lane * S < left ? (int)min((uint32_t)S, left - lane * S) : 0;
-        tp = warp_fold_slots<S, 1>(
-            tp, cnt, nsl, 0u, 0u, [&](int sl, int) { return s_w[wb][st][lane * S + sl]; },
-            [&](int l, int sl, int) { return s_w[wb][st][l * S + sl]; },
-            [](int, int, double xin) -> double { return xin; },
-            [&](int sl, double v) {
-                st_relaxed_u64(&tl[q0 + lane * S + sl], (uint64_t)__double_as_longlong(v));
-            });
+        if (__shfl_sync(kFull, failed, 0)) return;
+        double tp = __longlong_as_double((long long)__shfl_sync(kFull, (unsigned long long)tb, 0));
+        constexpr int S = kDownSlots;
+        constexpr uint32_t per_round = 32 * S;
+        const uint32_t nrounds = (end - q + per_round - 1) / per_round;
+        auto issue = [&](uint32_t r) {                   // one commit group per round
+            if (r < nrounds) {
+    #pragma unroll
+                for (int sl = 0; sl < S; ++sl) {
+                    const uint32_t qq = q + r * per_round + lane * S + sl;
+                    if (qq < end) cp_async8(&s_w[wb][r % kStagesDown][lane * S + sl], &wl[qq]);
+                }
+            }
+            cp_async_commit();
+        };
+    #pragma unroll
+        for (int r = 0; r < kStagesDown - 1; ++r) issue(r);
+        for (uint32_t r = 0; r < nrounds; ++r) {
+            __syncwarp();                                // stage r - 1 is no longer read
+            issue(r + kStagesDown - 1);
+            cp_async_wait<kStagesDown - 1>();
+            __syncwarp();
+            const int st = r % kStagesDown;
+            const uint32_t q0 = q + r * per_round;
+            const uint32_t left = end - q0;
+            const int cnt = left < per_round ? (int)((left + S - 1) / S) : 32;
+            const int nsl = (uint32_t)lane * S < left ? (int)min((uint32_t)S, left - lane * S) : 0;
+            tp = warp_fold_slots<S, 1>(
+                tp, cnt, nsl, 0u, 0u, [&](int sl, int) { return s_w[wb][st][lane * S + sl]; },
+                [&](int l, int sl, int) { return s_w[wb][st][l * S + sl]; },
+                [](int, int, double xin) -> double { return xin; },
+                [&](int sl, double v) {
+                    st_relaxed_u64(&tl[q0 + lane * S + sl], (uint64_t)__double_as_longlong(v));
+                });
+        }
+        cp_async_wait<0>();
     }
-    cp_async_wait<0>();
 }
 
 // With slope limits the elevation clamp e_v <= e_parent + tan * len chains through
@@ -980,51 +1082,56 @@ __global__ void k_s_top_down_slope(TopDown td, const uint32_t* __restrict__ layo
                                    const uint32_t* __restrict__ clen,
                                    const uint32_t* __restrict__ cqp,
                                    const uint8_t* __restrict__ needl, double* __restrict__ tl,
-                                   double* __restrict__ el, int* td_done, int stamp,
-                                   uint32_t* meta) {
+                                   double* __restrict__ el, const uint32_t* __restrict__ corder,
+                                   int* td_done, int stamp, uint32_t* meta) {
     const int lane = threadIdx.x & 31;
-    const int wb = threadIdx.x >> 5;
-    const uint32_t c = blockIdx.x * kWalkWarps + wb;
     if (lane != 0) return;
-    if (c >= meta[kMetaChains] || ld_acquire(&td.flags[kError]) != 0) return;
-    const uint32_t off = coff[c], len = clen[c];
-    if (off + len > meta[kMetaNs] || len == 0) {
-        set_error(td.flags, kErrForest);
-        return;
-    }
-    const uint32_t end = off + len;
-    uint32_t q = off;
-    uint32_t p = td.next[layout[off]];
-    if (cqp[c] == kNone) {                 // the root was settled before the walk
-        p = layout[off];
-        q = off + 1;
-    } else {
-        uint32_t spins = 0;
-        const uint64_t t0 = global_ns();
-        const long long c0 = clock64();
-        while (ld_acquire(&td_done[p]) != stamp) {
-            if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
-                set_error(td.flags, kErrWait);
-                return;
-            }
-            __nanosleep(32);
+    const uint32_t nc = meta[kMetaChains];
+    // one thread per chain, claimed shallowest first (a chain waits only for its parent)
+    while (true) {
+        if (ld_acquire(&td.flags[kError]) != 0) return;
+        const uint32_t idx = atomicAdd(&meta[kMetaClaimDown], 1u);
+        if (idx >= nc) return;
+        const uint32_t c = corder[idx];
+        const uint32_t off = coff[c], len = clen[c];
+        if (off + len > meta[kMetaNs] || len == 0) {
+            set_error(td.flags, kErrForest);
+            return;
         }
-        record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
-        if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
+        const uint32_t end = off + len;
+        uint32_t q = off;
+        uint32_t p = td.next[layout[off]];
+        if (cqp[c] == kNone) {                 // the root was settled before the walk
+            p = layout[off];
+            q = off + 1;
+        } else {
+            uint32_t spins = 0;
+            const uint64_t t0 = global_ns();
+            const long long c0 = clock64();
+            while (ld_acquire(&td_done[p]) != stamp) {
+                if (++spins > kSpinLimit || ((spins & 255) == 0 && ld_acquire(&td.flags[kError]))) {
+                    set_error(td.flags, kErrWait);
+                    return;
+                }
+                __nanosleep(32);
+            }
+            record_chain_stat(meta, kMetaDownSlow, global_ns() - t0, (uint64_t)(clock64() - c0), len);
+            if (spins) atomicAdd(&meta[kMetaSpinDown], spins);
+        }
+        bool changed = false;
+        TRec rp = load_rec(&td.rec[p]);
+        for (; q < end; ++q) {
+            const uint32_t v = layout[q];
+            double e;
+            const double tp = settle(td, v, p, rp, &e, &changed);
+            rp = TRec{tp, e, rp.to, rp.eo};      // the basin outlet's values pass down
+            tl[q] = tp;
+            el[q] = e;
+            p = v;
+            if (needl[q]) st_release(&td_done[v], stamp);   // v's record written above
+        }
+        if (changed) td.flags[kChanged] = 1;
     }
-    bool changed = false;
-    TRec rp = load_rec(&td.rec[p]);
-    for (; q < end; ++q) {
-        const uint32_t v = layout[q];
-        double e;
-        const double tp = settle(td, v, p, rp, &e, &changed);
-        rp = TRec{tp, e, rp.to, rp.eo};      // the basin outlet's values pass down
-        tl[q] = tp;
-        el[q] = e;
-        p = v;
-        if (needl[q]) st_release(&td_done[v], stamp);   // v's record written above
-    }
-    if (changed) td.flags[kChanged] = 1;
 }
 
 // Skeleton response times and elevations back to site order (records and elevations;
@@ -1186,7 +1293,9 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     const unsigned g_low_s = coop_grid((const void*)k_low_top_down<true>, kRoundBlock, 2);
     // ordered compactions: one block range each, two blocks per SM
     const unsigned g_compact = coop_grid((const void*)k_collect_leaves, kRoundBlock, 2);
-    const unsigned g_chain = (a.kahn_min_width + kWalkWarps - 1) / kWalkWarps;
+    // persistent chain walkers: every warp resident (they wait on one another)
+    const unsigned g_chain = a.walk_grid;
+    const unsigned g_tree = coop_grid((const void*)k_s_chain_tree, kThreads, 4);
     const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
     TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.rec_t, a.elev, a.flags, a.tid, a.tchg};
@@ -1232,6 +1341,12 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     k_s_layout<<<gs, kThreads, 0, st>>>(a.slist, rk, a.cid, a.coff, a.layout, a.slot_chain, a.kslot,
                                         a.meta,
                                         a.flags);
+    e = coop_launch(k_s_chain_tree, g_tree, kThreads, st, (const uint32_t*)a.next,
+                    (const uint32_t*)a.layout, (const uint32_t*)a.coff, (const uint32_t*)a.sid,
+                    (const uint32_t*)a.kslot, (const uint32_t*)a.slot_chain, a.cpar1, a.cdep,
+                    a.cpar1 + a.kahn_min_width, a.cdep1, a.cqp, a.cpar, a.chist, a.corder,
+                    a.meta, a.flags);
+    if (e != cudaSuccess) return e;
     k_s_prepare<<<gs, kThreads, 0, st>>>(n, a.row, a.col, a.next, a.hgt, a.area, a.A, a.layout,
                                          a.slot_chain, a.coff, a.clen, a.cbot, a.rec, a.info,
                                          a.tokval, a.tok_cap, a.push_to,
@@ -1244,8 +1359,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
                     (const uint32_t*)a.hgt, a.area, a.A, (const uint32_t*)a.layout,
                     (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const SlotRec*)a.rec,
                     (const SlotInfo*)a.info, a.tokval, (const uint64_t*)a.push_to, a.pre,
-                    a.bu_done, a.stamp, a.meta,
-                    a.flags);
+                    (const uint32_t*)a.corder, a.bu_done, a.stamp, a.meta, a.flags);
     hk.end(hk.ctx, kcSkelUp, 0.0);
     if (e != cudaSuccess) return e;
 
@@ -1264,21 +1378,21 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     hk.end(hk.ctx, kcBasinBuild, 0.0);
 
     hk.begin(hk.ctx);
-    k_s_chain_roots<<<1, kRoundBlock, 0, st>>>(td, (const uint32_t*)a.layout,
-                                               (const uint32_t*)a.coff, (const uint32_t*)a.sid,
-                                               (const uint32_t*)a.kslot,
-                                               (const uint32_t*)a.slot_chain, a.cpar, a.cqp,
-                                               a.cbas, a.cto, a.ceo, a.pre, a.el, a.td_done,
-                                               a.stamp, (const uint32_t*)a.meta);
+    k_s_settle_roots<<<gs, kThreads, 0, st>>>(td, (const uint32_t*)a.layout,
+                                              (const uint32_t*)a.coff, (const uint32_t*)a.cqp,
+                                              a.cbas, a.cto, a.ceo, a.pre, a.el, a.td_done,
+                                              a.stamp, (const uint32_t*)a.meta);
+    k_s_root_values<<<gs, kThreads, 0, st>>>((const uint32_t*)a.cpar, a.cbas, a.cto, a.ceo,
+                                             (const uint32_t*)a.meta, (const int*)a.flags);
     if (a.slope) {
         e = coop_launch(k_s_top_down_slope, g_chain, kWalkWarps * 32, st, td,
                         (const uint32_t*)a.layout, (const uint32_t*)a.coff,
                         (const uint32_t*)a.clen, (const uint32_t*)a.cqp, (const uint8_t*)a.needl,
-                        a.pre, a.el, a.td_done, a.stamp, a.meta);
+                        a.pre, a.el, (const uint32_t*)a.corder, a.td_done, a.stamp, a.meta);
     } else {
         e = coop_launch(k_s_top_down, g_chain, kWalkWarps * 32, st, (const int*)a.flags,
                         (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const uint32_t*)a.cqp,
-                        (const double*)a.post, a.pre, a.meta);
+                        (const double*)a.post, a.pre, (const uint32_t*)a.corder, a.meta);
     }
     hk.end(hk.ctx, kcSkelDown, 0.0);
     if (e != cudaSuccess) return e;

@@ -47,6 +47,8 @@ enum Meta {
     kMetaSpinUp,       // wait iterations of the bottom-up chain hand-offs
     kMetaSpinDown,     // wait iterations of the top-down chain hand-offs
     kMetaMaxChain,     // longest skeleton chain
+    kMetaClaimUp,      // chains claimed by the bottom-up walkers
+    kMetaClaimDown,    // chains claimed by the top-down walkers
     kMetaTok,          // used entries of the donor-list buffer
     kMetaUpSlow,       // (2 words, u64) slowest bottom-up chain, packed by pack_chain_stat
     kMetaUpSlowHi,
@@ -128,8 +130,14 @@ struct BasinArgs {
     uint32_t* layout;
     uint32_t* slot_chain;   // layout slot -> chain
     uint32_t* kslot;        // skeleton index -> layout slot
-    uint32_t* cpar;         // per chain: root chain of its chain tree (scratch)
+    uint32_t* cpar;         // per chain: root chain of its chain tree
     uint32_t* cqp;          // per chain: layout slot of the site it hangs from, or kNone
+    uint32_t* cdep;         // per chain: depth below its root chain (pointer jumping, 2 buffers)
+    uint32_t* cpar1;
+    uint32_t* cdep1;
+    uint32_t* chist;        // per depth: chain count, then its first position in corder
+    uint32_t* corder;       // chains by depth, shallowest first: the walkers' claim order
+    uint32_t walk_grid;     // blocks of the persistent chain walkers (all co-resident)
     double* el;             // skeleton elevations in layout order (slope limits only)
     uint32_t* cbas;         // per chain: basin outlet, its response time and elevation
     double* cto;

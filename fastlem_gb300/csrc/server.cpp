@@ -90,11 +90,10 @@ struct fl_server {
 namespace {
 
 // An instance's device footprint before it exists: the measured size of an earlier
-// instance of the same model, else a bound from the site and slot counts (an instance
-// allocates about 330 B per site, 12 B per adjacency slot and under 1 MiB besides).
+// instance of the same model, else fl_model_device_bytes's bound.
 uint64_t footprint(const Model& m) {
     if (m.bytes) return m.bytes;
-    return 400ull * m.n + 16ull * m.col.size() + (1ull << 20);
+    return fl_model_device_bytes(m.n, m.col.size());
 }
 
 void drop_idle(fl_server* s, uint32_t model, fl_graph* g) {

@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -51,7 +52,21 @@ using namespace fl;
 constexpr double kEpsilon = 2.220446049250313e-16;   // f64::EPSILON
 // Kahn rounds stop when the ready frontier is narrower than this; it also bounds
 // the number of skeleton chains (one co-resident thread each).
-constexpr uint32_t kKahnMinWidth = 8192;
+// The Kahn rounds stop once fewer sites than this are ready; the rest (the deep part of
+// the rivers) goes to the skeleton chains, walked by persistent warps.
+constexpr uint32_t kKahnMinWidth = 16384;
+
+// kKahnMinWidth, or FL_KAHN_MIN_WIDTH from the environment (a tuning knob, read once).
+uint32_t kahn_min_width() {
+    static const uint32_t w = [] {
+        if (const char* env = std::getenv("FL_KAHN_MIN_WIDTH")) {
+            const long v = std::strtol(env, nullptr, 10);
+            if (v >= 256 && v <= (1l << 24)) return (uint32_t)v;
+        }
+        return kKahnMinWidth;
+    }();
+    return w;
+}
 
 thread_local std::string g_err;
 
@@ -290,7 +305,9 @@ struct fl_graph {
     double *d_pre = nullptr, *d_post = nullptr, *d_tokval = nullptr,
            *d_el = nullptr, *d_cto = nullptr, *d_ceo = nullptr;
     bool slope = false;
-    uint32_t *d_kslot = nullptr, *d_cpar = nullptr, *d_cqp = nullptr;
+    uint32_t *d_kslot = nullptr, *d_cpar = nullptr, *d_cqp = nullptr, *d_cdep = nullptr,
+             *d_cpar1 = nullptr, *d_cdep1 = nullptr, *d_chist = nullptr, *d_corder = nullptr;
+    uint32_t walk_grid = 0;
     fl::SlotRec* d_rec = nullptr;
     fl::SlotInfo* d_info = nullptr;
     uint8_t* d_needl = nullptr;
@@ -334,7 +351,8 @@ void free_graph(fl_graph* g) {
                     g->d_pre, g->d_post, g->d_rec, g->d_info, g->d_bu_done, g->d_td_need, g->d_td_done,
                     g->d_slot_chain, g->d_cbas, g->d_el, g->d_cto, g->d_ceo, g->d_perm, g->d_inv,
                     g->d_tokval, g->d_needl, g->d_push, g->d_rtime, g->d_kslot, g->d_cpar,
-                    g->d_cqp, g->d_trec, g->d_noise_idx, g->d_tid, g->d_tchg};
+                    g->d_cqp, g->d_trec, g->d_noise_idx, g->d_tid, g->d_tchg, g->d_cdep,
+                    g->d_cpar1, g->d_cdep1, g->d_chist, g->d_corder};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -401,7 +419,8 @@ void kresolve(fl_graph* g) {
 int alloc_workspace(fl_graph* g) {
     const uint32_t n = g->n;
     // the Kahn rounds stop once fewer sites are ready than walk warps fit on the GPU
-    g->kahn_min_width = std::min<uint32_t>(kKahnMinWidth, std::max<uint32_t>(256, fl::walk_capacity()));
+    g->kahn_min_width = kahn_min_width();
+    g->walk_grid = std::max<uint32_t>(1, fl::walk_capacity() / fl::kWalkWarps);
     FL_TRY(dalloc(&g->d_k, n));
     FL_TRY(dalloc(&g->d_u, n));
     FL_TRY(dalloc(&g->d_tan, n));
@@ -446,6 +465,11 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_kslot, n));
     FL_TRY(dalloc(&g->d_cpar, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_cqp, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_cdep, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_cpar1, 2ull * g->kahn_min_width));   // pointer-jumping buffers
+    FL_TRY(dalloc(&g->d_cdep1, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_chist, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_corder, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_el, n));
     FL_TRY(dalloc(&g->d_cbas, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_cto, g->kahn_min_width));
@@ -734,6 +758,12 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.kslot = g->d_kslot;
     a.cpar = g->d_cpar;
     a.cqp = g->d_cqp;
+    a.cdep = g->d_cdep;
+    a.cpar1 = g->d_cpar1;
+    a.cdep1 = g->d_cdep1;
+    a.chist = g->d_chist;
+    a.corder = g->d_corder;
+    a.walk_grid = g->walk_grid;
     a.rec = g->d_rec;
     a.info = g->d_info;
     a.needl = g->d_needl;
@@ -1030,6 +1060,15 @@ int fl_batch_create(uint32_t terrains, const uint32_t* site_off, const uint32_t*
 uint32_t fl_graph_num_terrains(const fl_graph* g) { return g ? g->terrains : 0; }
 
 uint64_t fl_graph_device_bytes(const fl_graph* g) { return g ? g->dev_bytes : 0; }
+
+uint64_t fl_model_device_bytes(uint32_t n, uint64_t nnz) {
+    // per site about 330 B of arrays (per-site state, lake ranks, basin workspace,
+    // operand and top-down records, donor lists), per slot the CSR's 12 B; per-chain
+    // tables of kahn_min_width entries (64 B each), per-round tables and status words
+    const uint64_t width = kahn_min_width();
+    const uint64_t rounds = n / width + 64;
+    return 360ull * n + 12ull * nnz + 64ull * width + 24ull * rounds + 4096;
+}
 
 int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
                       const double* erodibility, const double* uplift, const uint8_t* is_outlet,

@@ -28,6 +28,9 @@ class TerrainServer:
         check(lib().fl_server_create(int(hbm_budget_bytes), int(slots), ctypes.byref(h)))
         self._h = h
         self._models = []
+        # every submitted request's buffers stay referenced here until it is waited for
+        # (or the server is closed): the workers write into them
+        self._pending = {}
 
     def add_model(self, model: TerrainModel2D) -> int:
         mid = ctypes.c_uint32()
@@ -53,7 +56,9 @@ class TerrainServer:
         if rc in _GEN_ERR:
             raise GenerationError(_GEN_ERR[rc])
         check(rc)
-        return Ticket(t.value, m, out, (p,))
+        ticket = Ticket(t.value, m, out, (p,))
+        self._pending[ticket.id] = ticket
+        return ticket
 
     def wait(self, ticket: Ticket):
         """(Terrain2D, {"iterations", "latency_ms", "queue_ms", "solve_ms"})"""
@@ -61,6 +66,7 @@ class TerrainServer:
         lat, qu, so = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         rc = lib().fl_server_wait(self._h, ticket.id, ctypes.byref(it), ctypes.byref(lat),
                                   ctypes.byref(qu), ctypes.byref(so))
+        self._pending.pop(ticket.id, None)
         if rc in _GEN_ERR:
             raise GenerationError(_GEN_ERR[rc])
         check(rc)
@@ -77,9 +83,11 @@ class TerrainServer:
         return dict(zip(self.STATS, (int(x) for x in out)))
 
     def close(self):
+        """Stops the server after the requests it is running; waiting ones are dropped."""
         if self._h is not None:
-            lib().fl_server_destroy(self._h)
+            lib().fl_server_destroy(self._h)   # joins the workers: no buffer is written after
             self._h = None
+            self._pending.clear()
 
     def __enter__(self):
         return self

@@ -114,6 +114,10 @@ uint32_t fl_graph_num_terrains(const fl_graph* g);
 /* Device memory a model holds (graph and workspace), in bytes. */
 uint64_t fl_graph_device_bytes(const fl_graph* g);
 
+/* An upper bound on fl_graph_device_bytes for a model of n sites and nnz adjacency
+ * slots, before it is created (HBM planning; the served form's admission). */
+uint64_t fl_model_device_bytes(uint32_t n, uint64_t nnz);
+
 /* generate() for every packed terrain at once: per-site parameters over all sites, one
  * max_iteration for all.  out_terrain_iterations[t] = the loop bodies terrain t would
  * have run alone (its first iteration without an elevation change, or the limit);

@@ -36,8 +36,12 @@ def solo(m, p, cap):
 def test_requests_in_the_mix_equal_alone(requests, budget_models, slots):
     cap = 30
     want = [solo(m, p, cap) for m, p in requests]
-    bytes_max = max(lib().fl_graph_device_bytes(m.handle()) for m, _ in requests)
-    budget = 120 * 10**9 if budget_models is None else budget_models * bytes_max + (1 << 20)
+    # room for `budget_models` of the largest instance (admission reserves the bound
+    # fl_model_device_bytes until an instance exists, then its measured size)
+    bound = max(lib().fl_model_device_bytes(m.n, int(m.row_ptr[-1])) for m, _ in requests)
+    real = max(lib().fl_graph_device_bytes(m.handle()) for m, _ in requests)
+    assert real <= bound
+    budget = 120 * 10**9 if budget_models is None else budget_models * bound
     with TerrainServer(hbm_budget_bytes=budget, slots=slots) as srv:
         ids = [srv.add_model(m) for m, _ in requests]
         # every model twice, interleaved: resident instances get reused
