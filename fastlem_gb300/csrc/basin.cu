@@ -48,6 +48,8 @@ constexpr uint32_t kTok = 2;       // donor list in tokval (a confluence with an
                                    // predecessor)
 constexpr uint32_t kSlow = 4;      // donor list too long: full pull at walk time
 constexpr int kPostShift = 3;      // bits 3-4: additions after the chain predecessor
+constexpr uint32_t kPend = 32;     // confluence whose operands (pre, posts) the last chain
+                                   // bottom to arrive computes from the donor list
 constexpr int kMaxPost = 3;
 constexpr int kTokCntShift = 8;    // bits 8-11: donor-list length (cell area first)
 constexpr int kHeavyShift = 12;    // bits 12-15: the predecessor's index in the list
@@ -364,10 +366,13 @@ __device__ __forceinline__ uint32_t grouped_add(uint32_t* base, uint32_t key, bo
 
 // The chain tree (cooperative).  A chain's parent is the chain holding the site its
 // bottom drains to (itself for a chain that ends at a root).  Pointer jumping gives every
-// chain its root chain (cpar) and depth; a counting sort by depth gives corder, the
-// shallowest chains first.  A chain only ever waits for its children (bottom-up: the
-// chains ending on it) or its parent (top-down), so walkers that claim chains deepest
-// first (bottom-up) or shallowest first (top-down) never wait for an unclaimed chain.
+// chain its root chain (cpar) and the depth of its bottom in sites below the root (a
+// child's bottom lies one site below a site of its parent, so it is strictly deeper than
+// the parent's bottom); a counting sort by that depth gives corder, shallowest first.
+// A chain only ever waits for its children (bottom-up: the chains ending on it) or its
+// parent (top-down), so walkers that claim chains deepest first (bottom-up) or shallowest
+// first (top-down) never wait for an unclaimed chain; the top-down order also claims
+// chains about when their parent's walk reaches them.
 __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t* __restrict__ layout,
                                const uint32_t* __restrict__ coff, const uint32_t* __restrict__ sid,
                                const uint32_t* __restrict__ kslot,
@@ -379,19 +384,21 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
     const uint32_t stride = gridDim.x * blockDim.x;
     if (ld_acquire(&flags[kError])) return;
     const uint32_t nc = meta[kMetaChains];
+    const uint32_t ns = meta[kMetaNs];
+    for (uint32_t i = gtid; i <= ns; i += stride) hist[i] = 0;
     for (uint32_t c = gtid; c < nc; c += stride) {
         const uint32_t v = layout[coff[c]];
         const uint32_t p = next[v];
-        hist[c] = 0;
         if (p == v) {
             par0[c] = c;
             dep0[c] = 0;
             cqp[c] = kNone;
         } else {
             const uint32_t q = kslot[sid[p]];
+            const uint32_t pc = slot_chain[q];
             cqp[c] = q;
-            par0[c] = slot_chain[q];
-            dep0[c] = 1;
+            par0[c] = pc;
+            dep0[c] = q - coff[pc] + 1;          // sites from the parent's bottom
         }
     }
     if (!grid_barrier(flags)) return;
@@ -413,17 +420,22 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
         const uint32_t c = base + threadIdx.x;
         const bool act = c < nc;
         const uint32_t d = act ? din[c] : 0;
+        bool bad = false;
         if (act) {
             cpar[c] = pin[c];
-            if (d >= nc || pin[pin[c]] != pin[c]) set_error(flags, kErrForest);
+            bad = d >= ns || pin[pin[c]] != pin[c];
+            if (bad) set_error(flags, kErrForest);
         }
-        grouped_add(hist, act ? d : 0, act);
+        grouped_add(hist, act && !bad ? d : 0, act && !bad);
+        const uint32_t dm = __reduce_max_sync(0xffffffffu, act && !bad ? d : 0);
+        if ((threadIdx.x & 31) == 0) atomicMax(&meta[kMetaMaxDepth], dm);
     }
     if (!grid_barrier(flags)) return;
     if (blockIdx.x == 0) {                       // exclusive scan of the depth counts
         __shared__ uint32_t part[1024];
-        const uint32_t per = (nc + blockDim.x - 1) / blockDim.x;
-        const uint32_t b = threadIdx.x * per, e = min(nc, b + per);
+        const uint32_t nb = meta[kMetaMaxDepth] + 1;
+        const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
+        const uint32_t b = threadIdx.x * per, e = min(nb, b + per);
         uint32_t sum = 0;
         for (uint32_t i = b; i < e; ++i) sum += hist[i];
         part[threadIdx.x] = sum;
@@ -444,7 +456,7 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
     if (!grid_barrier(flags)) return;
     for (uint32_t base = blockIdx.x * blockDim.x; base < nc; base += stride) {
         const uint32_t c = base + threadIdx.x;
-        const bool act = c < nc;
+        const bool act = c < nc && din[c] < ns;
         const uint32_t pos = grouped_add(hist, act ? din[c] : 0, act);
         if (act) corder[pos] = c;
     }
@@ -462,6 +474,7 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
                             const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
                             const uint32_t* __restrict__ cbot, SlotRec* __restrict__ rec,
                             SlotInfo* __restrict__ info, double* __restrict__ tokval,
+                            uint32_t* __restrict__ tokslot, uint32_t* __restrict__ pend,
                             uint32_t tok_cap, uint64_t* __restrict__ push_to,
                             int* __restrict__ td_need, int stamp, uint32_t* meta,
                             int* flags) {
@@ -524,7 +537,7 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
                 toff = 0;
             } else {
                 tokval[toff] = area[v];
-                uint32_t t = 1, hpos = 0;
+                uint32_t t = 1, hpos = 0, npend = 0;
                 for (uint32_t s = s1; s-- > s0;) {
                     uint32_t d = col[s];
                     if (d == v || next[d] != v) continue;
@@ -534,19 +547,35 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
                     } else if (hgt[d] == kNone) {
                         val = __longlong_as_double((long long)kPendingBits);
                         push_to[d] = ((uint64_t)(uint32_t)stamp << 32) | (toff + t);
+                        tokslot[toff + t] = q;
+                        ++npend;
                     } else {
                         val = A[d];
                     }
                     tokval[toff + t] = val;
                     ++t;
                 }
-                f |= kTok | (nt << kTokCntShift) | (hpos << kHeavyShift);
+                f |= (nt << kTokCntShift) | (hpos << kHeavyShift);
+                const uint32_t npost = hpos ? nt - 1 - hpos : 0;
+                if (hpos && npend && npost <= (uint32_t)kMaxPost) {
+                    // an ordinary fold slot once its operands arrive: the last chain
+                    // bottom to push computes pre and the posts from the list
+                    f |= kPend;
+                    pend[q] = npend;
+                    np = (int)npost;
+                    const double m = __longlong_as_double((long long)kPendingBits);
+                    a = m;
+                    ps[0] = ps[1] = ps[2] = m;
+                } else {
+                    f |= kTok;
+                    np = 0;
+                }
             }
-            np = 0;
+            if (!(f & kPend)) np = 0;
         }
         rec[q] = SlotRec{a, ps[0], ps[1], ps[2]};
         info[q] = SlotInfo{f | ((uint32_t)np << kPostShift), toff};
-        warp_append(&meta[kMetaSlow], (f & (kTok | kSlow)) != 0);
+        warp_append(&meta[kMetaSlow], (f & (kTok | kSlow | kPend)) != 0);
     }
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         uint32_t b = cbot[c];
@@ -632,6 +661,40 @@ __device__ __forceinline__ void st_relaxed_u64(double* p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+__device__ __forceinline__ uint64_t ld_acquire_u64(const double* p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// The last chain bottom to push into confluence slot q's donor list computes q's fold
+// operands from it (by the whole warp): pre = cell area + the donors before the chain
+// predecessor, in order, and the donors after it as posts; pre, stored last, is the
+// flag the slot's walker waits for.
+__device__ void finalize_pending(SlotRec* rec, const SlotInfo* info, const double* tokval,
+                                 uint32_t q) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t fl = info[q].flags, toff = info[q].tokoff;
+    const uint32_t nt = (fl >> kTokCntShift) & 15u, hpos = (fl >> kHeavyShift) & 15u;
+    double v = 0.0;
+    if ((uint32_t)lane < nt) v = __longlong_as_double((long long)ld_relaxed_u64(&tokval[toff + lane]));
+    double acc = __shfl_sync(0xffffffffu, v, 0);
+    for (uint32_t t = 1; t < hpos; ++t) acc = __dadd_rn(acc, __shfl_sync(0xffffffffu, v, t));
+    const double p0 = __shfl_sync(0xffffffffu, v, (hpos + 1) & 31);
+    const double p1 = __shfl_sync(0xffffffffu, v, (hpos + 2) & 31);
+    const double p2 = __shfl_sync(0xffffffffu, v, (hpos + 3) & 31);
+    if (lane == 0) {
+        const uint32_t npost = nt - 1 - hpos;
+        if (npost > 0) st_relaxed_u64(&rec[q].p0, (uint64_t)__double_as_longlong(p0));
+        if (npost > 1) st_relaxed_u64(&rec[q].p1, (uint64_t)__double_as_longlong(p1));
+        if (npost > 2) st_relaxed_u64(&rec[q].p2, (uint64_t)__double_as_longlong(p2));
+        __threadfence();
+        uint64_t ab = (uint64_t)__double_as_longlong(acc);
+        if (isnan(acc)) ab = 0x7ff8000000000000ull;   // never the pending marker
+        st_relaxed_u64(&rec[q].pre, ab);
+    }
+}
+
 // The full pull of a slot with a donor list, by the whole warp: lane t takes entry t
 // (waiting for a chain bottom's push), then the entries are added in order to the cell
 // area, x standing in for the chain predecessor.
@@ -702,8 +765,9 @@ k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col
               const uint32_t* __restrict__ next, const uint32_t* __restrict__ hgt,
               const double* __restrict__ area, double* A, const uint32_t* __restrict__ layout,
               const uint32_t* __restrict__ coff, const uint32_t* __restrict__ clen,
-              const SlotRec* __restrict__ rec, const SlotInfo* __restrict__ info,
-              double* tokval, const uint64_t* __restrict__ push_to, double* __restrict__ Al,
+              SlotRec* rec, const SlotInfo* __restrict__ info, double* tokval,
+              const uint32_t* __restrict__ tokslot, uint32_t* pend,
+              const uint64_t* __restrict__ push_to, double* __restrict__ Al,
               const uint32_t* __restrict__ corder, int* bu_done, int stamp, uint32_t* meta,
               int* flags) {
     constexpr int S = kUpSlots;
@@ -772,6 +836,44 @@ k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col
                     if (fl & (kLeafSlot | kTok | kSlow)) specm |= 1u << sl;
                 }
             }
+            // confluences finalised by the chain bottoms ending there: wait (bounded) for
+            // their operands if this round's copy predates them
+            bool pend_fail = false;
+#pragma unroll
+            for (int sl = 0; sl < S; ++sl) {
+                if (sl < nsl && (s_info[wb][st][lane * S + sl].flags & kPend)) {
+                    SlotRec& sr = s_rec[wb][st][lane * S + sl];
+                    const uint32_t npost = (s_info[wb][st][lane * S + sl].flags >> kPostShift) & 3u;
+                    const auto pending = [](double x) {
+                        return (uint64_t)__double_as_longlong(x) == kPendingBits;
+                    };
+                    if (pending(sr.pre) || (npost > 0 && pending(sr.p0)) ||
+                        (npost > 1 && pending(sr.p1)) || (npost > 2 && pending(sr.p2))) {
+                        const uint32_t q = top - (r * per_round + lane * S + sl);
+                        uint32_t sp = 0;
+                        uint64_t b = ld_acquire_u64(&rec[q].pre);
+                        while (b == kPendingBits) {
+                            if (++sp > kSpinLimit || ((sp & 255) == 0 && ld_acquire(&flags[kError]))) {
+                                set_error(flags, kErrWait);
+                                pend_fail = true;
+                                break;
+                            }
+                            __nanosleep(32);
+                            b = ld_acquire_u64(&rec[q].pre);
+                        }
+                        spins += sp;
+                        sr.pre = __longlong_as_double((long long)b);
+                        sr.p0 = __longlong_as_double((long long)ld_relaxed_u64(&rec[q].p0));
+                        sr.p1 = __longlong_as_double((long long)ld_relaxed_u64(&rec[q].p1));
+                        sr.p2 = __longlong_as_double((long long)ld_relaxed_u64(&rec[q].p2));
+                    }
+                }
+            }
+            if (__any_sync(kFull, pend_fail)) {
+                ok = false;
+                break;
+            }
+            __syncwarp();
             auto opnd = [&](int l, int sl, int j) -> double {
                 return reinterpret_cast<const double*>(&s_rec[wb][st][l * S + sl])[j];
             };
@@ -803,6 +905,7 @@ k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col
         }
         cp_async_wait<0>();                              // nothing in flight at exit
         if (!ok) return;
+        uint32_t fin = kNone;
         if (lane == 0) {
             uint32_t bottom = layout[off];
             A[bottom] = x;
@@ -812,8 +915,18 @@ k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col
                 uint64_t xb = (uint64_t)__double_as_longlong(x);
                 if (isnan(x)) xb = 0x7ff8000000000000ull;   // never the pending marker
                 st_relaxed_u64(&tokval[(uint32_t)pt], xb);
+                const uint32_t q = tokslot[(uint32_t)pt];
+                if (info[q].flags & kPend) {
+                    __threadfence();                          // the push, before the count
+                    if (atomicSub(&pend[q], 1u) == 1u) {
+                        __threadfence();                      // every push, before the reads
+                        fin = q;
+                    }
+                }
             }
         }
+        fin = __shfl_sync(kFull, fin, 0);
+        if (fin != kNone) finalize_pending(rec, info, tokval, fin);
         spins = __reduce_add_sync(kFull, spins);
         if (lane == 0 && spins) atomicAdd(&meta[kMetaSpinUp], spins);
         if (lane == 0)
@@ -1349,7 +1462,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     if (e != cudaSuccess) return e;
     k_s_prepare<<<gs, kThreads, 0, st>>>(n, a.row, a.col, a.next, a.hgt, a.area, a.A, a.layout,
                                          a.slot_chain, a.coff, a.clen, a.cbot, a.rec, a.info,
-                                         a.tokval, a.tok_cap, a.push_to,
+                                         a.tokval, a.tokslot, a.pend, a.tok_cap, a.push_to,
                                          a.td_need, a.stamp, a.meta, a.flags);
     hk.end(hk.ctx, kcBasinBuild, 0.0);
 
@@ -1357,9 +1470,10 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     hk.begin(hk.ctx);
     e = coop_launch(k_s_bottom_up, g_chain, kWalkWarps * 32, st, a.row, a.col, a.next,
                     (const uint32_t*)a.hgt, a.area, a.A, (const uint32_t*)a.layout,
-                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, (const SlotRec*)a.rec,
-                    (const SlotInfo*)a.info, a.tokval, (const uint64_t*)a.push_to, a.pre,
-                    (const uint32_t*)a.corder, a.bu_done, a.stamp, a.meta, a.flags);
+                    (const uint32_t*)a.coff, (const uint32_t*)a.clen, a.rec,
+                    (const SlotInfo*)a.info, a.tokval, (const uint32_t*)a.tokslot, a.pend,
+                    (const uint64_t*)a.push_to, a.pre, (const uint32_t*)a.corder, a.bu_done,
+                    a.stamp, a.meta, a.flags);
     hk.end(hk.ctx, kcSkelUp, 0.0);
     if (e != cudaSuccess) return e;
 

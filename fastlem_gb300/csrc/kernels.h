@@ -50,6 +50,8 @@ enum Meta {
     kMetaClaimUp,      // chains claimed by the bottom-up walkers
     kMetaClaimDown,    // chains claimed by the top-down walkers
     kMetaTok,          // used entries of the donor-list buffer
+    kMetaMaxDepth,     // largest chain-bottom depth (sites from the root)
+    kMetaPad3,
     kMetaUpSlow,       // (2 words, u64) slowest bottom-up chain, packed by pack_chain_stat
     kMetaUpSlowHi,
     kMetaDownSlow,     // (2 words, u64) slowest top-down chain, packed by pack_chain_stat
@@ -132,10 +134,11 @@ struct BasinArgs {
     uint32_t* kslot;        // skeleton index -> layout slot
     uint32_t* cpar;         // per chain: root chain of its chain tree
     uint32_t* cqp;          // per chain: layout slot of the site it hangs from, or kNone
-    uint32_t* cdep;         // per chain: depth below its root chain (pointer jumping, 2 buffers)
+    uint32_t* cdep;         // per chain: its bottom's depth in sites below the root (pointer
+                            // jumping, 2 buffers)
     uint32_t* cpar1;
     uint32_t* cdep1;
-    uint32_t* chist;        // per depth: chain count, then its first position in corder
+    uint32_t* chist;        // per depth (n + 1 entries): chain count, then first position in corder
     uint32_t* corder;       // chains by depth, shallowest first: the walkers' claim order
     uint32_t walk_grid;     // blocks of the persistent chain walkers (all co-resident)
     double* el;             // skeleton elevations in layout order (slope limits only)
@@ -148,7 +151,9 @@ struct BasinArgs {
     double* pre;            // layout-order areas (bottom-up), response times (top-down)
     double* post;           // layout-order w (top-down)
     uint8_t* needl;         // per layout slot: another chain starts below this site
-    double* tokval;         // donor lists: final donor areas, chain bottoms pushed at walk time
+    double* tokval;
+    uint32_t* tokslot;      // per donor-list entry: the slot whose list it is
+    uint32_t* pend;         // per layout slot: chain bottoms still to push into its list         // donor lists: final donor areas, chain bottoms pushed at walk time
     uint32_t tok_cap;
     uint64_t* push_to;      // per site: (stamp << 32) | tokval index its chain bottom fills
     int* bu_done;

@@ -310,6 +310,7 @@ struct fl_graph {
     uint32_t walk_grid = 0;
     fl::SlotRec* d_rec = nullptr;
     fl::SlotInfo* d_info = nullptr;
+    uint32_t *d_tokslot = nullptr, *d_pend = nullptr;
     uint8_t* d_needl = nullptr;
     uint64_t* d_push = nullptr;
     uint32_t tok_cap = 0;
@@ -352,7 +353,7 @@ void free_graph(fl_graph* g) {
                     g->d_slot_chain, g->d_cbas, g->d_el, g->d_cto, g->d_ceo, g->d_perm, g->d_inv,
                     g->d_tokval, g->d_needl, g->d_push, g->d_rtime, g->d_kslot, g->d_cpar,
                     g->d_cqp, g->d_trec, g->d_noise_idx, g->d_tid, g->d_tchg, g->d_cdep,
-                    g->d_cpar1, g->d_cdep1, g->d_chist, g->d_corder};
+                    g->d_cpar1, g->d_cdep1, g->d_chist, g->d_corder, g->d_tokslot, g->d_pend};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -468,7 +469,7 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_cdep, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_cpar1, 2ull * g->kahn_min_width));   // pointer-jumping buffers
     FL_TRY(dalloc(&g->d_cdep1, g->kahn_min_width));
-    FL_TRY(dalloc(&g->d_chist, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_chist, n + 1ull));
     FL_TRY(dalloc(&g->d_corder, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_el, n));
     FL_TRY(dalloc(&g->d_cbas, g->kahn_min_width));
@@ -484,6 +485,8 @@ int alloc_workspace(fl_graph* g) {
     // hold every list at once
     g->tok_cap = (uint32_t)std::min<uint64_t>(2ull * n + 64, 0xfffffff0ull);
     FL_TRY(dalloc(&g->d_tokval, g->tok_cap));
+    FL_TRY(dalloc(&g->d_tokslot, g->tok_cap));
+    FL_TRY(dalloc(&g->d_pend, n));
     FL_TRY(dalloc(&g->d_bu_done, n));
     FL_TRY(dalloc(&g->d_td_need, n));
     FL_TRY(dalloc(&g->d_td_done, n));
@@ -768,6 +771,8 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.info = g->d_info;
     a.needl = g->d_needl;
     a.tokval = g->d_tokval;
+    a.tokslot = g->d_tokslot;
+    a.pend = g->d_pend;
     a.tok_cap = g->tok_cap;
     a.push_to = g->d_push;
     a.bu_done = g->d_bu_done;
@@ -1062,12 +1067,12 @@ uint32_t fl_graph_num_terrains(const fl_graph* g) { return g ? g->terrains : 0; 
 uint64_t fl_graph_device_bytes(const fl_graph* g) { return g ? g->dev_bytes : 0; }
 
 uint64_t fl_model_device_bytes(uint32_t n, uint64_t nnz) {
-    // per site about 330 B of arrays (per-site state, lake ranks, basin workspace,
+    // per site about 350 B of arrays (per-site state, lake ranks, basin workspace,
     // operand and top-down records, donor lists), per slot the CSR's 12 B; per-chain
     // tables of kahn_min_width entries (64 B each), per-round tables and status words
     const uint64_t width = kahn_min_width();
     const uint64_t rounds = n / width + 64;
-    return 360ull * n + 12ull * nnz + 64ull * width + 24ull * rounds + 4096;
+    return 384ull * n + 12ull * nnz + 64ull * width + 24ull * rounds + 4096;
 }
 
 int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
