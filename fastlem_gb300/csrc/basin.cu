@@ -364,22 +364,73 @@ __device__ __forceinline__ uint32_t grouped_add(uint32_t* base, uint32_t key, bo
     return b + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
+// Counting sort inside a cooperative kernel: positions of the chains c < nc by key[c]
+// (stable within a key is not needed), written to out.  hist must be zero on entry up
+// to the largest key, which the sort records in meta[maxslot].
+__device__ bool grid_counting_sort(const uint32_t* key, uint32_t nc, uint32_t* hist,
+                                   uint32_t* meta, int maxslot, uint32_t* __restrict__ out,
+                                   int* flags) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < nc; base += stride) {
+        const uint32_t c = base + threadIdx.x;
+        const bool act = c < nc;
+        const uint32_t k = act ? key[c] : 0;
+        grouped_add(hist, k, act);
+        const uint32_t km = __reduce_max_sync(0xffffffffu, k);
+        if ((threadIdx.x & 31) == 0) atomicMax(&meta[maxslot], km);
+    }
+    if (!grid_barrier(flags)) return false;
+    if (blockIdx.x == 0) {                       // exclusive scan of the key counts
+        __shared__ uint32_t part[1024];
+        const uint32_t nb = meta[maxslot] + 1;
+        const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
+        const uint32_t b = threadIdx.x * per, e = min(nb, b + per);
+        uint32_t sum = 0;
+        for (uint32_t i = b; i < e; ++i) sum += hist[i];
+        part[threadIdx.x] = sum;
+        __syncthreads();
+        for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+            const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+            __syncthreads();
+            part[threadIdx.x] += v;
+            __syncthreads();
+        }
+        uint32_t run = part[threadIdx.x] - sum;
+        for (uint32_t i = b; i < e; ++i) {
+            const uint32_t h = hist[i];
+            hist[i] = run;
+            run += h;
+        }
+    }
+    if (!grid_barrier(flags)) return false;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < nc; base += stride) {
+        const uint32_t c = base + threadIdx.x;
+        const bool act = c < nc;
+        const uint32_t pos = grouped_add(hist, act ? key[c] : 0, act);
+        if (act) out[pos] = c;
+    }
+    return grid_barrier(flags);
+}
+
 // The chain tree (cooperative).  A chain's parent is the chain holding the site its
 // bottom drains to (itself for a chain that ends at a root).  Pointer jumping gives every
 // chain its root chain (cpar) and the depth of its bottom in sites below the root (a
 // child's bottom lies one site below a site of its parent, so it is strictly deeper than
-// the parent's bottom); a counting sort by that depth gives corder, shallowest first.
+// the parent's bottom).  A chain's height is the depth of the deepest chain bottom in
+// its subtree minus its own depth: strictly smaller for every child than for its parent.
 // A chain only ever waits for its children (bottom-up: the chains ending on it) or its
-// parent (top-down), so walkers that claim chains deepest first (bottom-up) or shallowest
-// first (top-down) never wait for an unclaimed chain; the top-down order also claims
-// chains about when their parent's walk reaches them.
+// parent (top-down), so walkers that claim chains by ascending height (corder_up) or by
+// ascending depth (corder_down) never wait for an unclaimed chain.  By height, chains
+// without children come first and the long main stems last, by depth a chain is
+// claimed about when its parent's walk reaches it.
 __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t* __restrict__ layout,
                                const uint32_t* __restrict__ coff, const uint32_t* __restrict__ sid,
                                const uint32_t* __restrict__ kslot,
                                const uint32_t* __restrict__ slot_chain, uint32_t* par0,
                                uint32_t* dep0, uint32_t* par1, uint32_t* dep1,
                                uint32_t* __restrict__ cqp, uint32_t* cpar, uint32_t* hist,
-                               uint32_t* __restrict__ corder, uint32_t* meta, int* flags) {
+                               uint32_t* __restrict__ corder_down,
+                               uint32_t* __restrict__ corder_up, uint32_t* meta, int* flags) {
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
     if (ld_acquire(&flags[kError])) return;
@@ -402,7 +453,7 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
         }
     }
     if (!grid_barrier(flags)) return;
-    // ceil(log2(nc)) + 1 rounds reach every root (depths are below nc)
+    // ceil(log2(nc)) + 1 rounds reach every root
     int rounds = 1;
     while ((1u << (rounds - 1)) < nc && rounds < 32) ++rounds;
     uint32_t *pin = par0, *din = dep0, *pout = par1, *dout = dep1;
@@ -416,50 +467,33 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
         uint32_t* t = pin; pin = pout; pout = t;
         t = din; din = dout; dout = t;
     }
-    for (uint32_t base = blockIdx.x * blockDim.x; base < nc; base += stride) {
-        const uint32_t c = base + threadIdx.x;
-        const bool act = c < nc;
-        const uint32_t d = act ? din[c] : 0;
-        bool bad = false;
-        if (act) {
-            cpar[c] = pin[c];
-            bad = d >= ns || pin[pin[c]] != pin[c];
-            if (bad) set_error(flags, kErrForest);
-        }
-        grouped_add(hist, act && !bad ? d : 0, act && !bad);
-        const uint32_t dm = __reduce_max_sync(0xffffffffu, act && !bad ? d : 0);
-        if ((threadIdx.x & 31) == 0) atomicMax(&meta[kMetaMaxDepth], dm);
+    // root chains, consistency, and the subtree maxima start at the own depth
+    uint32_t* maxd = dout;
+    for (uint32_t c = gtid; c < nc; c += stride) {
+        cpar[c] = pin[c];
+        if (din[c] >= ns || pin[pin[c]] != pin[c]) set_error(flags, kErrForest);
+        maxd[c] = din[c];
     }
     if (!grid_barrier(flags)) return;
-    if (blockIdx.x == 0) {                       // exclusive scan of the depth counts
-        __shared__ uint32_t part[1024];
-        const uint32_t nb = meta[kMetaMaxDepth] + 1;
-        const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
-        const uint32_t b = threadIdx.x * per, e = min(nb, b + per);
-        uint32_t sum = 0;
-        for (uint32_t i = b; i < e; ++i) sum += hist[i];
-        part[threadIdx.x] = sum;
-        __syncthreads();
-        for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
-            const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
-            __syncthreads();
-            part[threadIdx.x] += v;
-            __syncthreads();
-        }
-        uint32_t run = part[threadIdx.x] - sum;
-        for (uint32_t i = b; i < e; ++i) {
-            const uint32_t h = hist[i];
-            hist[i] = run;
-            run += h;
+    if (ld_acquire(&flags[kError])) return;
+    // every chain raises its ancestors' subtree maximum to its depth; a walk stops at an
+    // ancestor that already holds at least as much (its setter raises the rest)
+    for (uint32_t c = gtid; c < nc; c += stride) {
+        const uint32_t d = din[c];
+        uint32_t q = cqp[c];
+        for (uint32_t hops = 0; q != kNone && hops < nc; ++hops) {
+            const uint32_t a = slot_chain[q];
+            if (atomicMax(&maxd[a], d) >= d) break;
+            q = cqp[a];
         }
     }
     if (!grid_barrier(flags)) return;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < nc; base += stride) {
-        const uint32_t c = base + threadIdx.x;
-        const bool act = c < nc && din[c] < ns;
-        const uint32_t pos = grouped_add(hist, act ? din[c] : 0, act);
-        if (act) corder[pos] = c;
-    }
+    for (uint32_t c = gtid; c < nc; c += stride) maxd[c] -= din[c];   // heights
+    if (!grid_counting_sort(din, nc, hist, meta, kMetaMaxDepth, corder_down, flags)) return;
+    const uint32_t top = meta[kMetaMaxDepth];
+    for (uint32_t i = gtid; i <= top; i += stride) hist[i] = 0;
+    if (!grid_barrier(flags)) return;
+    grid_counting_sort(maxd, nc, hist, meta, kMetaMaxHeight, corder_up, flags);
 }
 
 // Per skeleton site (layout slot q): the part of its pull that precedes the chain
@@ -776,15 +810,15 @@ k_s_bottom_up(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col
     const int lane = threadIdx.x & 31;
     const int wb = threadIdx.x >> 5;
     const uint32_t nc = meta[kMetaChains];
-    // persistent warps claim chains deepest first (a chain waits only for the chains
-    // ending on it, which are deeper); warp-uniform exits only
+    // persistent warps claim chains by ascending height (a chain waits only for the
+    // chains ending on it, whose heights are smaller); warp-uniform exits only
     while (true) {
         if (__any_sync(kFull, ld_acquire(&flags[kError]) != 0)) return;
         uint32_t idx = 0;
         if (lane == 0) idx = atomicAdd(&meta[kMetaClaimUp], 1u);
         idx = __shfl_sync(kFull, idx, 0);
         if (idx >= nc) return;
-        const uint32_t c = corder[nc - 1 - idx];
+        const uint32_t c = corder[idx];
         const uint32_t off = coff[c];
         const uint32_t len = clen[c];
         if (off + len > meta[kMetaNs] || len == 0) {
@@ -1458,7 +1492,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
                     (const uint32_t*)a.layout, (const uint32_t*)a.coff, (const uint32_t*)a.sid,
                     (const uint32_t*)a.kslot, (const uint32_t*)a.slot_chain, a.cpar1, a.cdep,
                     a.cpar1 + a.kahn_min_width, a.cdep1, a.cqp, a.cpar, a.chist, a.corder,
-                    a.meta, a.flags);
+                    a.corder_up, a.meta, a.flags);
     if (e != cudaSuccess) return e;
     k_s_prepare<<<gs, kThreads, 0, st>>>(n, a.row, a.col, a.next, a.hgt, a.area, a.A, a.layout,
                                          a.slot_chain, a.coff, a.clen, a.cbot, a.rec, a.info,
@@ -1472,7 +1506,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
                     (const uint32_t*)a.hgt, a.area, a.A, (const uint32_t*)a.layout,
                     (const uint32_t*)a.coff, (const uint32_t*)a.clen, a.rec,
                     (const SlotInfo*)a.info, a.tokval, (const uint32_t*)a.tokslot, a.pend,
-                    (const uint64_t*)a.push_to, a.pre, (const uint32_t*)a.corder, a.bu_done,
+                    (const uint64_t*)a.push_to, a.pre, (const uint32_t*)a.corder_up, a.bu_done,
                     a.stamp, a.meta, a.flags);
     hk.end(hk.ctx, kcSkelUp, 0.0);
     if (e != cudaSuccess) return e;

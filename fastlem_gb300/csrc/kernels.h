@@ -51,7 +51,7 @@ enum Meta {
     kMetaClaimDown,    // chains claimed by the top-down walkers
     kMetaTok,          // used entries of the donor-list buffer
     kMetaMaxDepth,     // largest chain-bottom depth (sites from the root)
-    kMetaPad3,
+    kMetaMaxHeight,    // largest chain height (sites)
     kMetaUpSlow,       // (2 words, u64) slowest bottom-up chain, packed by pack_chain_stat
     kMetaUpSlowHi,
     kMetaDownSlow,     // (2 words, u64) slowest top-down chain, packed by pack_chain_stat
@@ -139,7 +139,8 @@ struct BasinArgs {
     uint32_t* cpar1;
     uint32_t* cdep1;
     uint32_t* chist;        // per depth (n + 1 entries): chain count, then first position in corder
-    uint32_t* corder;       // chains by depth, shallowest first: the walkers' claim order
+    uint32_t* corder;       // chains by depth, shallowest first: the top-down claim order
+    uint32_t* corder_up;    // chains by height, lowest first: the bottom-up claim order
     uint32_t walk_grid;     // blocks of the persistent chain walkers (all co-resident)
     double* el;             // skeleton elevations in layout order (slope limits only)
     uint32_t* cbas;         // per chain: basin outlet, its response time and elevation

@@ -52,20 +52,30 @@ using namespace fl;
 constexpr double kEpsilon = 2.220446049250313e-16;   // f64::EPSILON
 // Kahn rounds stop when the ready frontier is narrower than this; it also bounds
 // the number of skeleton chains (one co-resident thread each).
-// The Kahn rounds stop once fewer sites than this are ready; the rest (the deep part of
-// the rivers) goes to the skeleton chains, walked by persistent warps.
-constexpr uint32_t kKahnMinWidth = 16384;
+// The Kahn rounds stop once fewer sites than this are ready (n / 512, between the two
+// bounds); the rest (the deep part of the rivers) goes to the skeleton chains, walked by
+// persistent warps.  Narrow rounds cost a grid barrier each, a wide skeleton costs its
+// build and the chain hand-offs.
+constexpr uint32_t kKahnMinWidth = 65536;
+constexpr uint32_t kKahnMinWidthLow = 8192;
+// ... and for the first passes of a generate(): the chains follow the largest drainage
+// area of the previous pass, which is only the cell area on the first pass and a poor
+// guide on the second, and a wide skeleton cut into badly chosen chains walks slowly.
+constexpr uint32_t kKahnMinWidthEarly = 8192;
+constexpr uint32_t kEarlyPasses = 2;
 
-// kKahnMinWidth, or FL_KAHN_MIN_WIDTH from the environment (a tuning knob, read once).
-uint32_t kahn_min_width() {
-    static const uint32_t w = [] {
+// The stop width for a model of n sites, or FL_KAHN_MIN_WIDTH from the environment (a
+// tuning knob, read once).
+uint32_t kahn_min_width(uint32_t n) {
+    static const uint32_t forced = [] {
         if (const char* env = std::getenv("FL_KAHN_MIN_WIDTH")) {
             const long v = std::strtol(env, nullptr, 10);
             if (v >= 256 && v <= (1l << 24)) return (uint32_t)v;
         }
-        return kKahnMinWidth;
+        return 0u;
     }();
-    return w;
+    if (forced) return forced;
+    return std::max(kKahnMinWidthLow, std::min(kKahnMinWidth, n / 512));
 }
 
 thread_local std::string g_err;
@@ -306,7 +316,8 @@ struct fl_graph {
            *d_el = nullptr, *d_cto = nullptr, *d_ceo = nullptr;
     bool slope = false;
     uint32_t *d_kslot = nullptr, *d_cpar = nullptr, *d_cqp = nullptr, *d_cdep = nullptr,
-             *d_cpar1 = nullptr, *d_cdep1 = nullptr, *d_chist = nullptr, *d_corder = nullptr;
+             *d_cpar1 = nullptr, *d_cdep1 = nullptr, *d_chist = nullptr, *d_corder = nullptr,
+             *d_corder_up = nullptr;
     uint32_t walk_grid = 0;
     fl::SlotRec* d_rec = nullptr;
     fl::SlotInfo* d_info = nullptr;
@@ -316,6 +327,7 @@ struct fl_graph {
     uint32_t tok_cap = 0;
     int *d_bu_done = nullptr, *d_td_need = nullptr, *d_td_done = nullptr;
     uint32_t max_rounds = 0, kahn_min_width = kKahnMinWidth;
+    uint32_t passes = 0;   // basin passes since the drainage areas were reset
     int stamp = 0;
     uint32_t last_meta[kMetaCount] = {};
     // instrumentation: launches / algorithmic bytes always, device time when enabled
@@ -353,7 +365,8 @@ void free_graph(fl_graph* g) {
                     g->d_slot_chain, g->d_cbas, g->d_el, g->d_cto, g->d_ceo, g->d_perm, g->d_inv,
                     g->d_tokval, g->d_needl, g->d_push, g->d_rtime, g->d_kslot, g->d_cpar,
                     g->d_cqp, g->d_trec, g->d_noise_idx, g->d_tid, g->d_tchg, g->d_cdep,
-                    g->d_cpar1, g->d_cdep1, g->d_chist, g->d_corder, g->d_tokslot, g->d_pend};
+                    g->d_cpar1, g->d_cdep1, g->d_chist, g->d_corder, g->d_tokslot, g->d_pend,
+                    g->d_corder_up};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -420,7 +433,7 @@ void kresolve(fl_graph* g) {
 int alloc_workspace(fl_graph* g) {
     const uint32_t n = g->n;
     // the Kahn rounds stop once fewer sites are ready than walk warps fit on the GPU
-    g->kahn_min_width = kahn_min_width();
+    g->kahn_min_width = kahn_min_width(n);
     g->walk_grid = std::max<uint32_t>(1, fl::walk_capacity() / fl::kWalkWarps);
     FL_TRY(dalloc(&g->d_k, n));
     FL_TRY(dalloc(&g->d_u, n));
@@ -446,7 +459,7 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_hgt, n));
     FL_TRY(dalloc(&g->d_order, n));
     // each Kahn round retires at least kahn_min_width sites
-    g->max_rounds = n / g->kahn_min_width + 64;
+    g->max_rounds = n / std::min(g->kahn_min_width, kKahnMinWidthEarly) + 64;
     FL_TRY(dalloc(&g->d_roff, g->max_rounds + 2));
     FL_TRY(dalloc(&g->d_rtime, 2ull * (g->max_rounds + 1)));
     FL_TRY(dalloc(&g->d_meta, kMetaCount));
@@ -471,6 +484,7 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_cdep1, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_chist, n + 1ull));
     FL_TRY(dalloc(&g->d_corder, g->kahn_min_width));
+    FL_TRY(dalloc(&g->d_corder_up, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_el, n));
     FL_TRY(dalloc(&g->d_cbas, g->kahn_min_width));
     FL_TRY(dalloc(&g->d_cto, g->kahn_min_width));
@@ -733,7 +747,10 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.roff = g->d_roff;
     a.rtime = g->d_rtime;
     a.max_rounds = g->max_rounds;
-    a.kahn_min_width = g->kahn_min_width;
+    a.kahn_min_width = g->passes < kEarlyPasses
+                           ? std::min(g->kahn_min_width, kKahnMinWidthEarly)
+                           : g->kahn_min_width;
+    g->passes++;
     a.meta = g->d_meta;
     a.flags = g->d_flags;
     a.tid = g->d_tid;
@@ -766,6 +783,7 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.cdep1 = g->d_cdep1;
     a.chist = g->d_chist;
     a.corder = g->d_corder;
+    a.corder_up = g->d_corder_up;
     a.walk_grid = g->walk_grid;
     a.rec = g->d_rec;
     a.info = g->d_info;
@@ -855,6 +873,7 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     if (max_iter > 0xffffffffll) max_iter = 0xffffffffll;
     uint64_t limit = max_iter < 0 ? 0xffffffffull : (uint64_t)max_iter;
     uint32_t iters = 0;
+    g->passes = 0;
     // a terrain alone stops at its first iteration without a change; packed with others
     // it keeps iterating at a fixed point, so its count is that first unchanged iteration
     std::vector<uint32_t> t_iters(g->terrains, 0);
@@ -1070,8 +1089,8 @@ uint64_t fl_model_device_bytes(uint32_t n, uint64_t nnz) {
     // per site about 350 B of arrays (per-site state, lake ranks, basin workspace,
     // operand and top-down records, donor lists), per slot the CSR's 12 B; per-chain
     // tables of kahn_min_width entries (64 B each), per-round tables and status words
-    const uint64_t width = kahn_min_width();
-    const uint64_t rounds = n / width + 64;
+    const uint64_t width = kahn_min_width(n);
+    const uint64_t rounds = n / std::min<uint64_t>(width, kKahnMinWidthEarly) + 64;
     return 384ull * n + 12ull * nnz + 64ull * width + 24ull * rounds + 4096;
 }
 
