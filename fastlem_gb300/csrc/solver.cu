@@ -240,6 +240,16 @@ __global__ void k_lake_flip(uint32_t n, const uint32_t* __restrict__ row,
     rlen[k] = edge_len_or_one(row, col, len, k, nk);
 }
 
+__global__ void k_fill_nan(uint32_t n, double* __restrict__ d) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = __longlong_as_double(0x7ff8000000000000ll);
+}
+
+__global__ void k_mark(uint32_t m, const uint32_t* __restrict__ ids, uint8_t* __restrict__ table) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) table[ids[i]] = 1;
+}
+
 // Response times out of the per-site top-down records (probes).
 __global__ void k_rec_times(uint32_t n, const fl::TRec* __restrict__ rec, double* __restrict__ t) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -581,12 +591,17 @@ int download_permuted(fl_graph* g, const double* src, double* dst) {
 // Uploads the outlet list and table, computing (or reusing) the lake-heap rank.
 int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_rank) {
     uint32_t n = g->n;
-    std::vector<uint8_t> table(n, 0);
-    for (uint32_t o : outlets) table[o] = 1;
-    FL_CU(cudaMemcpyAsync(g->d_outlet, table.data(), n, cudaMemcpyHostToDevice, g->stream));
-    if (!outlets.empty())
+    // the outlet table from the list, on the device
+    FL_CU(cudaMemsetAsync(g->d_outlet, 0, n, g->stream));
+    if (!outlets.empty()) {
         FL_CU(cudaMemcpyAsync(g->d_outlets, outlets.data(), outlets.size() * 4,
                               cudaMemcpyHostToDevice, g->stream));
+        k_mark<<<blocks_for((uint32_t)outlets.size()), kThreads, 0, g->stream>>>(
+            (uint32_t)outlets.size(), g->d_outlets, g->d_outlet);
+        FL_CU(cudaGetLastError());
+        // pageable copies return before the DMA ends: keep the list until it is done
+        FL_CU(cudaStreamSynchronize(g->stream));
+    }
     if (!g->rank_valid || g->rank_key != outlets) {
         g->rank_valid = false;
         g->rank_uploaded = false;
@@ -814,30 +829,29 @@ int run_basin_pass(fl_graph* g, int* changed) {
     return FL_OK;
 }
 
+// Parameters into device order.  The uploads share one staging buffer; stream order
+// makes each copy wait for the previous gather, and a copy from pageable memory has
+// taken its data by the time it returns, so no host synchronisation is needed.
+// tan(max_slope) is computed on the host with the C library's tan, as fastlem's
+// `max_slope.tan()` is; without any slope limit the device array is just NaN.
 int upload_params(fl_graph* g, const double* base, const double* k, const double* u,
                   const double* max_slope) {
     uint32_t n = g->n;
-    std::vector<double> tanv(n);
     g->slope = false;
-    for (uint32_t i = 0; i < n; ++i) {
-        tanv[i] = (max_slope && !std::isnan(max_slope[i])) ? std::tan(max_slope[i]) : NAN;
-        if (!std::isnan(tanv[i])) g->slope = true;
+    if (base) FL_TRY(upload_permuted(g, base, g->d_base));
+    if (k) FL_TRY(upload_permuted(g, k, g->d_k));
+    if (u) FL_TRY(upload_permuted(g, u, g->d_u));
+    if (max_slope)
+        for (uint32_t i = 0; i < n && !g->slope; ++i) g->slope = !std::isnan(max_slope[i]);
+    if (g->slope) {
+        std::vector<double> tanv(n);
+        for (uint32_t i = 0; i < n; ++i)
+            tanv[i] = std::isnan(max_slope[i]) ? NAN : std::tan(max_slope[i]);
+        FL_TRY(upload_permuted(g, tanv.data(), g->d_tan));
+    } else {
+        k_fill_nan<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_tan);
+        FL_CU(cudaGetLastError());
     }
-    // one staging buffer: each upload waits for the previous gather to consume it
-    if (base) {
-        FL_TRY(upload_permuted(g, base, g->d_base));
-        FL_CU(cudaStreamSynchronize(g->stream));
-    }
-    if (k) {
-        FL_TRY(upload_permuted(g, k, g->d_k));
-        FL_CU(cudaStreamSynchronize(g->stream));
-    }
-    if (u) {
-        FL_TRY(upload_permuted(g, u, g->d_u));
-        FL_CU(cudaStreamSynchronize(g->stream));
-    }
-    FL_TRY(upload_permuted(g, tanv.data(), g->d_tan));
-    FL_CU(cudaStreamSynchronize(g->stream));
     return FL_OK;
 }
 
