@@ -430,12 +430,15 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
                                uint32_t* dep0, uint32_t* par1, uint32_t* dep1,
                                uint32_t* __restrict__ cqp, uint32_t* cpar, uint32_t* hist,
                                uint32_t* __restrict__ corder_down,
-                               uint32_t* __restrict__ corder_up, uint32_t* meta, int* flags) {
+                               uint32_t* __restrict__ corder_up, uint32_t walkers, uint32_t* meta,
+                               int* flags) {
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
     if (ld_acquire(&flags[kError])) return;
     const uint32_t nc = meta[kMetaChains];
     const uint32_t ns = meta[kMetaNs];
+    // with a walker for every chain all chains run at once and their order is free
+    const bool sort = nc > walkers;
     for (uint32_t i = gtid; i <= ns; i += stride) hist[i] = 0;
     for (uint32_t c = gtid; c < nc; c += stride) {
         const uint32_t v = layout[coff[c]];
@@ -473,7 +476,9 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
         cpar[c] = pin[c];
         if (din[c] >= ns || pin[pin[c]] != pin[c]) set_error(flags, kErrForest);
         maxd[c] = din[c];
+        if (!sort) corder_down[c] = corder_up[c] = c;
     }
+    if (!sort) return;
     if (!grid_barrier(flags)) return;
     if (ld_acquire(&flags[kError])) return;
     // every chain raises its ancestors' subtree maximum to its depth; a walk stops at an
@@ -1492,7 +1497,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
                     (const uint32_t*)a.layout, (const uint32_t*)a.coff, (const uint32_t*)a.sid,
                     (const uint32_t*)a.kslot, (const uint32_t*)a.slot_chain, a.cpar1, a.cdep,
                     a.cpar1 + a.kahn_min_width, a.cdep1, a.cqp, a.cpar, a.chist, a.corder,
-                    a.corder_up, a.meta, a.flags);
+                    a.corder_up, a.walk_grid * kWalkWarps, a.meta, a.flags);
     if (e != cudaSuccess) return e;
     k_s_prepare<<<gs, kThreads, 0, st>>>(n, a.row, a.col, a.next, a.hgt, a.area, a.A, a.layout,
                                          a.slot_chain, a.coff, a.clen, a.cbot, a.rec, a.info,
