@@ -998,13 +998,50 @@ __global__ void k_s_gather_down(const uint32_t* __restrict__ layout, const doubl
     }
 }
 
-// w_v = (1 / (k_v * sqrt(A_v))) * len_v  (generator.rs:172-173)
+// w_v = (1 / (k_v * sqrt(A_v))) * len_v  (generator.rs:172-173).  The f64 square root
+// and divide bound this kernel, and after the first iterations of a solve most drainage
+// areas and receivers stay as they were: with `valid` (k unchanged since the previous
+// pass, whose w, A and len are in w / wa / wl) a site whose A and len have the same bits
+// keeps its w -- the same operands give the same result.  A warp issues its f64
+// sequence if any lane needs it, and changed sites are scattered, so each block first
+// packs its changed sites into shared memory and computes them on dense warps.
+// blockDim.x == kThreads.
 __global__ void k_w(uint32_t n, const double* __restrict__ A, const double* __restrict__ kk,
-                    const double* __restrict__ rlen, double* __restrict__ w) {
-    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
-    double cel = __dmul_rn(kk[v], __dsqrt_rn(A[v]));
-    w[v] = __dmul_rn(__ddiv_rn(1.0, cel), rlen[v]);
+                    const double* __restrict__ rlen, double* __restrict__ w,
+                    double* __restrict__ wa, double* __restrict__ wl, bool valid) {
+    __shared__ uint32_t s_site[kThreads];
+    __shared__ double s_a[kThreads], s_l[kThreads];
+    __shared__ uint32_t s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    bool need = false;
+    double a = 0.0, l = 0.0;
+    if (v < n) {
+        a = A[v];
+        l = rlen[v];
+        need = !valid || __double_as_longlong(a) != __double_as_longlong(wa[v]) ||
+               __double_as_longlong(l) != __double_as_longlong(wl[v]);
+    }
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    uint32_t base = 0;
+    if (lane == 0 && m) base = atomicAdd(&s_cnt, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (need) {
+        const uint32_t k = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        s_site[k] = v;
+        s_a[k] = a;
+        s_l[k] = l;
+    }
+    __syncthreads();
+    if (threadIdx.x >= s_cnt) return;
+    const uint32_t u = s_site[threadIdx.x];
+    const double au = s_a[threadIdx.x], lu = s_l[threadIdx.x];
+    const double cel = __dmul_rn(kk[u], __dsqrt_rn(au));
+    w[u] = __dmul_rn(__ddiv_rn(1.0, cel), lu);
+    wa[u] = au;
+    wl[u] = lu;
 }
 
 struct TopDown {
@@ -1041,11 +1078,13 @@ __device__ __forceinline__ TRec load_rec(const TRec* r) {
 // and v's own inputs (w, uplift, tan of the maximum slope, receiver distance, current
 // elevation, outlet flag).  Writes v's record -- the basin outlet's response time and
 // new elevation carried along, or kNoOutletBits for a basin without an outlet -- and,
-// in a basin with an outlet, its elevation.  Returns t_v.
+// in a basin with an outlet, its elevation.  Returns t_v.  A site that is nobody's
+// receiver may skip its record (write_rec false) unless the records are read back.
 __device__ __forceinline__ double settle_own(const TopDown& td, uint32_t v, bool root,
                                              const TRec& rp, double w, double u, double tn,
                                              double dist, double old_e, bool is_outlet,
-                                             double* e_out, bool* changed) {
+                                             double* e_out, bool* changed,
+                                             bool write_rec = true) {
     double tv, to, eo, ep;
     bool has_o;
     if (root) {                           // t = 0 + (0 + w), the outlet is v itself
@@ -1075,8 +1114,10 @@ __device__ __forceinline__ double settle_own(const TopDown& td, uint32_t v, bool
     // below a root the outlet's elevation is its updated one
     const double to_below = has_o ? to : __longlong_as_double((long long)kNoOutletBits);
     TRec out{tv, ne, to_below, root ? ne : eo};
-    reinterpret_cast<double2*>(&td.rec[v])[0] = make_double2(out.t, out.e);
-    reinterpret_cast<double2*>(&td.rec[v])[1] = make_double2(out.to, out.eo);
+    if (write_rec) {
+        reinterpret_cast<double2*>(&td.rec[v])[0] = make_double2(out.t, out.e);
+        reinterpret_cast<double2*>(&td.rec[v])[1] = make_double2(out.to, out.eo);
+    }
     *e_out = ne;
     return tv;
 }
@@ -1323,10 +1364,12 @@ __global__ void k_s_finish(TopDown td, const uint32_t* __restrict__ layout,
 // After the barrier a site only needs its receiver's record: each thread loads its
 // first site of the next round (id at the start of the round, receiver and own inputs
 // before the barrier), so a narrow round costs about one barrier and one load.
+// Round 0 is the leaves, which are nobody's receiver: their records are written only
+// when all_records asks for every site's record.
 template <bool kSlope>
 __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
                                const uint32_t* __restrict__ roff, uint64_t* __restrict__ rtime,
-                               const uint32_t* meta) {
+                               const uint32_t* meta, bool all_records) {
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
     if (ld_acquire(&td.flags[kError])) return;
@@ -1367,7 +1410,7 @@ __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
             if (f.p == f.v) f.outlet = td.outlet[f.v] != 0;
             double en;
             settle_own(td, f.v, f.p == f.v, rp, f.w, f.u, f.tn, f.dist, f.old_e, f.outlet, &en,
-                       &changed);
+                       &changed, r > 0 || all_records);
         }
         have = nv != kNone;
         if (have) inputs(nv, cur);
@@ -1522,7 +1565,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
 
     // w: A 8 + k 8 + rlen 8 + w 8 per site
     hk.begin(hk.ctx);
-    k_w<<<nb, kThreads, 0, st>>>(n, a.A, a.k, a.rlen, a.w);
+    k_w<<<nb, kThreads, 0, st>>>(n, a.A, a.k, a.rlen, a.w, a.w_area, a.w_dist, a.w_valid);
     hk.end(hk.ctx, kcW, 32.0 * n);
 
     hk.begin(hk.ctx);
@@ -1564,11 +1607,11 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     if (a.slope)
         e = coop_launch(k_low_top_down<true>, g_low_s, kRoundBlock, st, td,
                         (const uint32_t*)a.order, (const uint32_t*)a.roff,
-                        a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta);
+                        a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta, a.all_records);
     else
         e = coop_launch(k_low_top_down<false>, g_low, kRoundBlock, st, td,
                         (const uint32_t*)a.order, (const uint32_t*)a.roff,
-                        a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta);
+                        a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta, a.all_records);
     hk.end(hk.ctx, kcLowDown, 112.0 * n);
     return e;
 }

@@ -102,6 +102,10 @@ struct BasinArgs {
     double* A;
     TRec* rec_t;
     double* w;
+    double* w_area;            // the A and receiver distance each w was computed from
+    double* w_dist;
+    bool w_valid;              // w / w_area / w_dist hold the previous pass's values
+    bool all_records;          // every site's record is read afterwards (else leaves skip it)
     double* elev;
     uint32_t* pending;
     uint32_t* hgt;
@@ -152,9 +156,9 @@ struct BasinArgs {
     double* pre;            // layout-order areas (bottom-up), response times (top-down)
     double* post;           // layout-order w (top-down)
     uint8_t* needl;         // per layout slot: another chain starts below this site
-    double* tokval;
+    double* tokval;         // donor lists: final donor areas, chain bottoms pushed at walk time
     uint32_t* tokslot;      // per donor-list entry: the slot whose list it is
-    uint32_t* pend;         // per layout slot: chain bottoms still to push into its list         // donor lists: final donor areas, chain bottoms pushed at walk time
+    uint32_t* pend;         // per layout slot: chain bottoms still to push into its list
     uint32_t tok_cap;
     uint64_t* push_to;      // per site: (stamp << 32) | tokval index its chain bottom fills
     int* bu_done;
@@ -174,8 +178,10 @@ struct Hooks {
 void set_last_error(const char* msg);
 
 void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const uint32_t* col,
-                      const double* len, const double* elev, const uint8_t* outlet,
-                      uint32_t* next, double* rlen, int* flags);
+                      const double* len, const float* ilen, const double* elev,
+                      const uint8_t* outlet, uint32_t* next, double* rlen, int* flags);
+// ilen[s] = 1/len[s] in f32 (NaN where not a normal f32), for launch_receivers.
+void launch_inv_len(cudaStream_t st, uint64_t nnz, const double* len, float* ilen);
 
 // Runs the exact parallel fold over one chain of n operands starting at x0 (probe).
 cudaError_t fold_probe(const double* y, uint32_t n, double x0, double* out);

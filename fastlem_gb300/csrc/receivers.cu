@@ -8,13 +8,20 @@
 // straightforward scan FP64-bound.  Here every candidate's slope is first estimated
 // in f32 from the exact bit patterns:
 //   * e_i > e_j is an integer comparison of the bit patterns (both non-negative);
-//   * d = e_i - e_j is formed in 64-bit integers, exactly when the exponents differ
-//     by <= 11 and truncated (error < 2^-52 relative) otherwise, then cut to 24 bits;
-//   * the slope estimate d_f / len_f has relative error below 2^-20.
+//   * d = e_i - e_j: when both share a binary exponent (the usual case for
+//     neighbours) the bit patterns' difference is the exact difference in units of
+//     that exponent's ulp, converted to f32 within 2^-23 relative; otherwise it is formed
+//     in 64-bit integers, exactly when the exponents differ by <= 11 and truncated
+//     (error < 2^-52 relative) otherwise, then cut to 24 bits;
+//   * the estimate is d times the slot's 1/len, rounded to f32 once per graph, so it
+//     has relative error below 2^-20.
 // If the largest estimate exceeds every other by more than a factor (1 - 2^-17)^-1,
 // its exact slope is strictly the largest, so it is the reference's receiver.
 // Otherwise (near-ties, negative or non-finite values, values outside the f32
 // range) the row is rescanned exactly as the reference does.
+
+#include <algorithm>
+#include <cfloat>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -54,29 +61,34 @@ __device__ __forceinline__ bool diff_estimate(uint64_t A, uint64_t B, float& out
     return true;
 }
 
-// Float estimate of a positive finite double (truncated mantissa).
-__device__ __forceinline__ bool to_float_estimate(uint64_t L, float& out) {
-    int e = (int)(L >> 52);
-    if ((L >> 63) || e == 0 || e == 0x7ff) return false;
-    int fe = e - 1023 + 127;
-    if (fe <= 0 || fe >= 255) return false;
-    out = __uint_as_float(((uint32_t)fe << 23) | (uint32_t)((L >> 29) & 0x7fffffu));
-    return true;
+// f32 estimate of a - b for non-negative finite doubles with bits A > B.  Sharing
+// the exponent field e in [949, 1149], A - B is the difference in units of 2^(e-1075)
+// (below 2^52) and the scaled result is a normal f32 number.  The 52-bit difference is
+// converted as two 32-bit halves (a 64-bit integer conversion issues on the f64 pipe):
+// the high half is exact, the low half truncated and the fused sum rounded, within
+// 2^-23 relative.
+__device__ __forceinline__ bool slope_diff(uint64_t A, uint64_t B, float& out) {
+    const uint32_t e = (uint32_t)(A >> 52);
+    if (e == (uint32_t)(B >> 52) && e - 949u <= 200u) {
+        const uint64_t D = A - B;
+        const float d = fmaf(__uint2float_rz((uint32_t)(D >> 32)), 4294967296.0f,
+                             __uint2float_rz((uint32_t)D));
+        out = d * __uint_as_float((e - 948u) << 23);
+        return true;
+    }
+    return diff_estimate(A, B, out);
 }
 
-__device__ __forceinline__ void scan_site(uint32_t i, const uint32_t* __restrict__ row,
+// Site i's receiver and receiver distance.  s0 / s1 bound its row; dmax is the
+// largest row length (up to kRowFast) among the warp's sites on the short-row path,
+// so the unrolled gathers stop where the warp's rows do.
+__device__ __forceinline__ void scan_site(uint32_t i, uint32_t s0, uint32_t s1, uint32_t dmax,
                                           const uint32_t* __restrict__ col,
                                           const double* __restrict__ len,
+                                          const float* __restrict__ ilen,
                                           const double* __restrict__ elev,
-                                          const uint8_t* __restrict__ outlet,
                                           uint32_t* __restrict__ next, double* __restrict__ rlen,
                                           bool* lake, bool* went_exact) {
-    if (outlet[i]) {
-        next[i] = i;
-        rlen[i] = 1.0;
-        return;
-    }
-    const uint32_t s0 = row[i], s1 = row[i + 1];
     const double ei = elev[i];
     const uint64_t EI = (uint64_t)__double_as_longlong(ei);
     bool exact = (EI >> 63) != 0 || (EI >> 52) == 0x7ff;   // negative or non-finite
@@ -90,13 +102,12 @@ __device__ __forceinline__ void scan_site(uint32_t i, const uint32_t* __restrict
             if ((EJ >> 63) || (EJ >> 52) == 0x7ff) { exact = true; return; }
             if (EI <= EJ) return;                          // not lower (bits are monotone)
             any_lower = true;
-            float d, l;
-            if (!diff_estimate(EI, EJ, d) ||
-                !to_float_estimate((uint64_t)__double_as_longlong(len[s]), l)) {
+            float d;
+            if (!slope_diff(EI, EJ, d)) {
                 exact = true;
                 return;
             }
-            float a = __fdividef(d, l);
+            const float a = d * ilen[s];
             if (!(a > 1e-30f) || !(a < 1e30f)) { exact = true; return; }
             if (a > best) {
                 second = best;
@@ -112,21 +123,26 @@ __device__ __forceinline__ void scan_site(uint32_t i, const uint32_t* __restrict
             uint32_t jj[kRowFast];
             uint64_t ej[kRowFast];
 #pragma unroll
-            for (int k = 0; k < kRowFast; ++k)
+            for (int k = 0; k < kRowFast; ++k) {
+                if ((uint32_t)k >= dmax) break;
                 if ((uint32_t)k < deg) jj[k] = col[s0 + k];
+            }
 #pragma unroll
-            for (int k = 0; k < kRowFast; ++k)
+            for (int k = 0; k < kRowFast; ++k) {
+                if ((uint32_t)k >= dmax) break;
                 if ((uint32_t)k < deg) ej[k] = (uint64_t)__double_as_longlong(elev[jj[k]]);
+            }
 #pragma unroll
-            for (int k = 0; k < kRowFast; ++k)
+            for (int k = 0; k < kRowFast; ++k) {
+                if ((uint32_t)k >= dmax) break;
                 if ((uint32_t)k < deg) consider(s0 + k, ej[k]);
+            }
         } else {
             for (uint32_t s = s0; s < s1; ++s)
                 consider(s, (uint64_t)__double_as_longlong(elev[col[s]]));
         }
         if (!exact && any_lower && second > best * (1.0f - 7.62939453125e-06f)) exact = true;
     }
-    uint32_t nb = i;
     if (exact) {
         *went_exact = true;
         double steepest = 0.0;
@@ -149,33 +165,62 @@ __device__ __forceinline__ void scan_site(uint32_t i, const uint32_t* __restrict
         *lake = true;
         return;
     }
-    nb = col[best_slot];
-    next[i] = nb;
-    uint32_t s = s0;
-    while (col[s] != nb) ++s;   // first entry of the receiver, as has_edge reports it
-    rlen[i] = len[s];
+    // A duplicate of the receiver later in the row has the same slope and never wins
+    // (strictly larger only; in the estimate it is a near-tie), so best_slot is the
+    // receiver's first entry, the one has_edge reports.
+    next[i] = col[best_slot];
+    rlen[i] = len[best_slot];
 }
 
 
 __global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
                             const uint32_t* __restrict__ col, const double* __restrict__ len,
-                            const double* __restrict__ elev, const uint8_t* __restrict__ outlet,
-                            uint32_t* __restrict__ next, double* __restrict__ rlen,
-                            int* __restrict__ flags) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool lake = false, went_exact = false;
-    if (i < n) scan_site(i, row, col, len, elev, outlet, next, rlen, &lake, &went_exact);
+                            const float* __restrict__ ilen, const double* __restrict__ elev,
+                            const uint8_t* __restrict__ outlet, uint32_t* __restrict__ next,
+                            double* __restrict__ rlen, int* __restrict__ flags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool lake = false, went_exact = false, scan = false;
+    uint32_t s0 = 0, s1 = 0;
+    if (i < n) {
+        if (outlet[i]) {
+            next[i] = i;
+            rlen[i] = 1.0;
+        } else {
+            s0 = row[i];
+            s1 = row[i + 1];
+            scan = true;
+        }
+    }
+    const uint32_t deg = s1 - s0;
+    const uint32_t dmax = __reduce_max_sync(0xffffffffu, deg <= (uint32_t)kRowFast ? deg : 0u);
+    if (scan) scan_site(i, s0, s1, dmax, col, len, ilen, elev, next, rlen, &lake, &went_exact);
     block_flag(flags, kHasLake, lake);
     if (__syncthreads_or(went_exact) && threadIdx.x == 0) atomicAdd(&flags[kExact], 1);
+}
+
+// 1/len per slot in f32 for the slope estimates, NaN where that is not a normal f32
+// number (the row then takes the exact scan).
+__global__ void k_inv_len(uint64_t nnz, const double* __restrict__ len, float* __restrict__ ilen) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < nnz;
+         s += (uint64_t)gridDim.x * blockDim.x) {
+        const float f = __double2float_rn(__ddiv_rn(1.0, len[s]));
+        ilen[s] = (f >= FLT_MIN && f <= FLT_MAX) ? f : __int_as_float(0x7fc00000);
+    }
 }
 
 }  // namespace
 
 void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const uint32_t* col,
-                      const double* len, const double* elev, const uint8_t* outlet,
-                      uint32_t* next, double* rlen, int* flags) {
-    k_receivers<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(n, row, col, len, elev, outlet,
-                                                                     next, rlen, flags);
+                      const double* len, const float* ilen, const double* elev,
+                      const uint8_t* outlet, uint32_t* next, double* rlen, int* flags) {
+    k_receivers<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(n, row, col, len, ilen, elev,
+                                                                     outlet, next, rlen, flags);
+}
+
+void launch_inv_len(cudaStream_t st, uint64_t nnz, const double* len, float* ilen) {
+    if (nnz == 0) return;
+    const uint64_t blocks = std::min<uint64_t>((nnz + kThreads - 1) / kThreads, 152ull * 64);
+    k_inv_len<<<(unsigned)blocks, kThreads, 0, st>>>(nnz, len, ilen);
 }
 
 }  // namespace fl

@@ -306,9 +306,14 @@ struct fl_graph {
     // model (device)
     uint32_t *d_row = nullptr, *d_col = nullptr;
     double *d_len = nullptr, *d_area = nullptr;
+    float* d_ilen = nullptr;   // 1/len per slot in f32 (receiver slope estimates)
     // parameters and iteration state (device)
     double *d_k = nullptr, *d_u = nullptr, *d_tan = nullptr, *d_base = nullptr, *d_elev = nullptr,
-           *d_A = nullptr, *d_t = nullptr, *d_w = nullptr, *d_rlen = nullptr;
+           *d_A = nullptr, *d_t = nullptr, *d_w = nullptr, *d_rlen = nullptr,
+           *d_wa = nullptr, *d_wl = nullptr;
+    // d_w / d_wa / d_wl hold the last pass's w and the A and receiver distance it came
+    // from, for the current parameters (cleared whenever d_w is reused or k uploaded)
+    bool w_valid = false;
     uint32_t *d_next = nullptr, *d_lab = nullptr, *d_lab2 = nullptr, *d_rank = nullptr,
              *d_sor = nullptr, *d_outlets = nullptr, *d_bas = nullptr;
     uint8_t* d_outlet = nullptr;
@@ -376,7 +381,7 @@ void free_graph(fl_graph* g) {
                     g->d_tokval, g->d_needl, g->d_push, g->d_rtime, g->d_kslot, g->d_cpar,
                     g->d_cqp, g->d_trec, g->d_noise_idx, g->d_tid, g->d_tchg, g->d_cdep,
                     g->d_cpar1, g->d_cdep1, g->d_chist, g->d_corder, g->d_tokslot, g->d_pend,
-                    g->d_corder_up};
+                    g->d_corder_up, g->d_wa, g->d_wl, g->d_ilen};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
@@ -453,6 +458,8 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_A, n));
     FL_TRY(dalloc(&g->d_t, n));
     FL_TRY(dalloc(&g->d_w, n));
+    FL_TRY(dalloc(&g->d_wa, n));
+    FL_TRY(dalloc(&g->d_wl, n));
     FL_TRY(dalloc(&g->d_rlen, n));
     FL_TRY(dalloc(&g->d_next, n));
     FL_TRY(dalloc(&g->d_lab, n));
@@ -582,6 +589,7 @@ int upload_permuted(fl_graph* g, const double* src, double* dst) {
 int download_permuted(fl_graph* g, const double* src, double* dst) {
     // w is dead after a pass (and response times must survive the downloads)
     double* stage = (src == g->d_w) ? g->d_t : g->d_w;
+    if (stage == g->d_w) g->w_valid = false;
     k_gather_f64<<<blocks_for(g->n), kThreads, 0, g->stream>>>(g->n, g->d_inv, src, stage);
     FL_CU(cudaGetLastError());
     FL_CU(cudaMemcpyAsync(dst, stage, g->n * 8ull, cudaMemcpyDeviceToHost, g->stream));
@@ -658,8 +666,8 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
 int run_receivers(fl_graph* g, int* has_lake) {
     FL_TRY(clear_flags(g));
     FL_LAUNCH(g, kcReceivers, 25.0 * g->n + 20.0 * g->nnz,
-              fl::launch_receivers(g->stream, g->n, g->d_row, g->d_col, g->d_len, g->d_elev,
-                                   g->d_outlet, g->d_next, g->d_rlen, g->d_flags));
+              fl::launch_receivers(g->stream, g->n, g->d_row, g->d_col, g->d_len, g->d_ilen,
+                                   g->d_elev, g->d_outlet, g->d_next, g->d_rlen, g->d_flags));
     FL_CU(cudaGetLastError());
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
@@ -732,7 +740,8 @@ void account_skeleton(fl_graph* g) {
     g->k_bytes[kcSkelRank] += 24.0 * ns * rounds;
 }
 
-int run_basin_pass(fl_graph* g, int* changed) {
+// all_records: every site's top-down record is read afterwards (response times)
+int run_basin_pass(fl_graph* g, int* changed, bool all_records = false) {
     FL_TRY(clear_flags(g));
     g->stamp = g->stamp == 0x7ffffff0 ? 1 : g->stamp + 1;
     if (g->stamp == 1) {   // stamps wrapped (or first pass): clear hand-off words
@@ -755,6 +764,10 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.A = g->d_A;
     a.rec_t = g->d_trec;
     a.w = g->d_w;
+    a.w_area = g->d_wa;
+    a.w_dist = g->d_wl;
+    a.w_valid = g->w_valid;
+    g->w_valid = false;   // until the pass, and with it k_w, has run
     a.elev = g->d_elev;
     a.pending = g->d_pending;
     a.hgt = g->d_hgt;
@@ -812,6 +825,7 @@ int run_basin_pass(fl_graph* g, int* changed) {
     a.td_need = g->d_td_need;
     a.td_done = g->d_td_done;
     a.stamp = g->stamp;
+    a.all_records = all_records;
     fl::Hooks hk{g, kbegin, kend};
     cudaError_t e = fl::basin_pass(a, g->stream, hk, (uint32_t)std::min<uint64_t>(g->nnz, 0xffffffffu));
     if (e != cudaSuccess) {
@@ -824,6 +838,7 @@ int run_basin_pass(fl_graph* g, int* changed) {
     int h[kNumFlags];
     FL_TRY(read_flags(g, h));
     FL_TRY(device_error(h));
+    g->w_valid = true;
     account_skeleton(g);
     *changed = h[kChanged];
     return FL_OK;
@@ -839,7 +854,10 @@ int upload_params(fl_graph* g, const double* base, const double* k, const double
     uint32_t n = g->n;
     g->slope = false;
     if (base) FL_TRY(upload_permuted(g, base, g->d_base));
-    if (k) FL_TRY(upload_permuted(g, k, g->d_k));
+    if (k) {
+        FL_TRY(upload_permuted(g, k, g->d_k));
+        g->w_valid = false;
+    }
     if (u) FL_TRY(upload_permuted(g, u, g->d_u));
     if (max_slope)
         for (uint32_t i = 0; i < n && !g->slope; ++i) g->slope = !std::isnan(max_slope[i]);
@@ -875,6 +893,7 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     // every terrain draws its own StdRng::seed_from_u64(0) stream, sample i for its site i
     FL_LAUNCH(g, kcNoise, 8.0 * g->noise_n,
               k_noise<<<blocks_for((g->noise_n + 7) / 8), kThreads, 0, g->stream>>>(g->noise_n, g->d_w));
+    g->w_valid = false;
     FL_LAUNCH(g, kcNoise, 28.0 * n,
               k_initial_elevation<<<blocks_for(n), kThreads, 0, g->stream>>>(
                   n, g->d_noise_idx ? g->d_noise_idx : g->d_perm, g->d_base, g->d_w, g->d_elev));
@@ -1038,7 +1057,8 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
         return fail(FL_ERR_CUDA);
     }
     if ((rc = dalloc(&g->d_row, n + 1)) || (rc = dalloc(&g->d_col, nnz)) ||
-        (rc = dalloc(&g->d_len, nnz)) || (rc = dalloc(&g->d_area, n)) ||
+        (rc = dalloc(&g->d_len, nnz)) || (rc = dalloc(&g->d_ilen, nnz)) ||
+        (rc = dalloc(&g->d_area, n)) ||
         (rc = dalloc(&g->d_perm, n)) || (rc = dalloc(&g->d_inv, n)) || (rc = alloc_workspace(g)))
         return fail(rc);
     if (cudaMemcpy(g->d_row, g->h_row.data(), (n + 1) * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1048,6 +1068,17 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
         cudaMemcpy(g->d_perm, g->perm.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(g->d_inv, g->inv.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) {
         g_err = "graph upload failed";
+        return fail(FL_ERR_CUDA);
+    }
+    // the copies above ran on the default stream: let them land before the solver's
+    // stream reads the lengths
+    if (cudaStreamSynchronize(0) != cudaSuccess) {
+        g_err = "graph upload failed";
+        return fail(FL_ERR_CUDA);
+    }
+    fl::launch_inv_len(g->stream, nnz, g->d_len, g->d_ilen);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(g->stream) != cudaSuccess) {
+        g_err = "inverse edge lengths failed";
         return fail(FL_ERR_CUDA);
     }
     if (k_terr > 1) {
@@ -1100,12 +1131,12 @@ uint32_t fl_graph_num_terrains(const fl_graph* g) { return g ? g->terrains : 0; 
 uint64_t fl_graph_device_bytes(const fl_graph* g) { return g ? g->dev_bytes : 0; }
 
 uint64_t fl_model_device_bytes(uint32_t n, uint64_t nnz) {
-    // per site about 350 B of arrays (per-site state, lake ranks, basin workspace,
-    // operand and top-down records, donor lists), per slot the CSR's 12 B; per-chain
+    // per site about 370 B of arrays (per-site state, lake ranks, basin workspace,
+    // operand and top-down records, donor lists), per slot the CSR's 12 B and 4 B of 1/len; per-chain
     // tables of kahn_min_width entries (64 B each), per-round tables and status words
     const uint64_t width = kahn_min_width(n);
     const uint64_t rounds = n / std::min<uint64_t>(width, kKahnMinWidthEarly) + 64;
-    return 384ull * n + 12ull * nnz + 64ull * width + 24ull * rounds + 4096;
+    return 400ull * n + 16ull * nnz + 64ull * width + 24ull * rounds + 4096;
 }
 
 int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
@@ -1210,7 +1241,7 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
     FL_CU(cudaStreamSynchronize(g->stream));
     int ch = 0;
-    FL_TRY(run_basin_pass(g, &ch));
+    FL_TRY(run_basin_pass(g, &ch, true));
     FL_TRY(download_permuted(g, g->d_elev, elev));
     FL_CU(cudaStreamSynchronize(g->stream));
     if (drainage_out) {
@@ -1219,6 +1250,7 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     }
     if (response_out) {
         k_rec_times<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_trec, g->d_w);
+        g->w_valid = false;
         FL_TRY(download_permuted(g, g->d_w, response_out));
         FL_CU(cudaStreamSynchronize(g->stream));
     }

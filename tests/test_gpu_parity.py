@@ -100,6 +100,57 @@ def test_receivers_parity(orc, name, g):
             assert bool(hl.value) == has_lake
 
 
+def _hard_elevations(rng, n, family):
+    """Elevations that stress the receivers' f32 slope estimates."""
+    if family == "offset":        # one binary exponent, differences ~1e-9 of the value
+        return 1000.0 + rng.uniform(0, 1e-6, n)
+    if family == "binades":       # around powers of two: neighbours in different binades
+        return np.ldexp(1.0, rng.integers(-3, 4, n)) * (1.0 + rng.uniform(-1e-6, 1e-6, n))
+    if family == "extreme":       # far outside the f32 range, subnormals, zeros
+        pick = rng.integers(0, 6, n)
+        vals = np.array([0.0, 5e-324, 1e-300, 1e300, 1e-40, 3e38])
+        return vals[pick] * (1.0 + rng.uniform(0, 1e-3, n))
+    # special values scattered over a smooth field
+    e = rng.uniform(0, 1, n)
+    pick = rng.integers(0, 40, n)
+    e[pick == 0] = np.nan
+    e[pick == 1] = np.inf
+    e[pick == 2] = -np.inf
+    e[pick == 3] = -rng.uniform(0, 1, int((pick == 3).sum()))
+    e[pick == 4] = 0.0
+    e[pick == 5] = -0.0
+    return e
+
+
+@pytest.mark.parametrize("family", ["offset", "binades", "extreme", "special"])
+@pytest.mark.parametrize("lengths", ["plain", "degenerate"])
+def test_receivers_parity_hard_values(orc, family, lengths):
+    g = graphs.random_delaunay(3000, seed=21)
+    if lengths == "degenerate":
+        # zero, subnormal, tiny and huge edge lengths (rows then take the exact scan)
+        rng = np.random.default_rng(4)
+        ln = g.length.copy()
+        pick = rng.integers(0, 30, len(ln))
+        ln[pick == 0] = 0.0
+        ln[pick == 1] = 1e-310
+        ln[pick == 2] = 1e-45
+        ln[pick == 3] = 1e300
+        ln[pick == 4] = 1e39
+        g = graphs.Graph(g.n, g.row_ptr, g.col, ln, g.area, g.default_outlets, g.xs, g.ys)
+    rng = np.random.default_rng(17)
+    with Handle(g) as h:
+        for trial in range(3):
+            elev = _hard_elevations(rng, g.n, family)
+            table = (rng.uniform(size=g.n) < 0.05).astype(np.uint8)
+            want = orc.initial_tree(g, elev, table)
+            got = np.empty(g.n, np.uint32)
+            hl = ctypes.c_int()
+            check(lib().fl_probe_receivers(h.h, ptr(elev), ptr(table), ptr(got), ctypes.byref(hl)))
+            assert np.array_equal(got, want), f"{family}/{lengths} trial {trial}"
+            _, has_lake = orc.roots(table, want)
+            assert bool(hl.value) == has_lake
+
+
 @pytest.mark.parametrize("name,g", CASES, ids=[c[0] for c in CASES])
 def test_lake_rerouting_parity(orc, name, g):
     rng = np.random.default_rng(9)
