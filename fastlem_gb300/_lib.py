@@ -31,7 +31,7 @@ EXPORTS = [
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
     "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate", "fl_graph_device_bytes",
-    "fl_model_device_bytes",
+    "fl_model_device_bytes", "fl_host_alloc", "fl_host_free",
     "fl_server_create", "fl_server_add_model", "fl_server_submit", "fl_server_wait",
     "fl_server_stats", "fl_server_destroy",
     "fl_probe_receivers", "fl_probe_lakes", "fl_probe_tree_pass", "fl_probe_prim_rank",
@@ -70,6 +70,9 @@ def lib():
     L.fl_graph_device_bytes.restype = c_u64
     L.fl_model_device_bytes.argtypes = [c_u32, c_u64]
     L.fl_model_device_bytes.restype = c_u64
+    L.fl_host_alloc.argtypes = [c_u64, P(vp)]
+    L.fl_host_free.argtypes = [vp]
+    L.fl_host_free.restype = None
     L.fl_server_create.argtypes = [c_u64, c_u32, P(vp)]
     L.fl_server_add_model.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, c_u32, vp, vp, P(c_u32)]
     L.fl_server_submit.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, ctypes.c_int64, vp, P(c_u64)]
@@ -125,6 +128,31 @@ def ptr(a):
         return None
     assert a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(vp)
+
+
+class _PinnedBlock:
+    """Owner of one fl_host_alloc block; freed when the last array over it is gone."""
+
+    def __init__(self, nbytes):
+        p = vp()
+        check(lib().fl_host_alloc(nbytes, ctypes.byref(p)))
+        self.p = p.value
+
+    def __del__(self):
+        if self.p and _lib is not None:
+            _lib.fl_host_free(vp(self.p))
+            self.p = None
+
+
+def pinned_empty(n, dtype):
+    """An uninitialised 1-D numpy array of n elements in page-locked host memory
+    (fl_host_alloc): host<->device copies of it run by DMA at the link's rate."""
+    dtype = np.dtype(dtype)
+    nbytes = max(1, int(n) * dtype.itemsize)
+    block = _PinnedBlock(nbytes)
+    raw = (ctypes.c_uint8 * nbytes).from_address(block.p)
+    raw._block = block               # the buffer keeps its block alive
+    return np.frombuffer(raw, dtype=dtype, count=int(n))
 
 
 def as_u32(a):

@@ -22,7 +22,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import as_f64, as_u32, as_u8, check, lib, ptr
+from ._lib import as_f64, as_u32, as_u8, check, lib, pinned_empty, ptr
 
 
 class GenerationError(Exception):
@@ -118,6 +118,19 @@ class ParameterArrays:
 
     def __len__(self):
         return len(self.base)
+
+    def pinned(self) -> "ParameterArrays":
+        """A copy whose arrays live in page-locked host memory, so generate() uploads
+        them by DMA, overlapped with its host-side work."""
+        q = ParameterArrays.__new__(ParameterArrays)
+        for name in ("base", "erodibility", "uplift", "is_outlet", "max_slope"):
+            a = getattr(self, name)
+            if a is not None:
+                b = pinned_empty(len(a), a.dtype)
+                b[:] = a
+                a = b
+            setattr(q, name, a)
+        return q
 
     @staticmethod
     def from_list(params: Sequence[TopographicalParameters]) -> "ParameterArrays":
@@ -362,7 +375,9 @@ class TerrainGenerator:
         self.max_iteration = int(max_iteration)
         return self
 
-    def generate(self) -> Terrain2D:
+    def generate(self, out=None) -> Terrain2D:
+        """`out`: optional float64 array of num() sites that receives the elevations
+        (e.g. one from pinned_empty, reused across calls); the result wraps it."""
         # error order as generator.rs:91-116
         if self.model is None:
             raise GenerationError("ModelNotSet")
@@ -374,7 +389,10 @@ class TerrainGenerator:
         m = self.model
         if len(p) != m.num():
             raise GenerationError("InvalidNumberOfParameters")
-        out = np.empty(m.num(), np.float64)
+        if out is None:
+            out = np.empty(m.num(), np.float64)
+        elif out.dtype != np.float64 or out.shape != (m.num(),) or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float64 array of num() elements")
         iters = ctypes.c_uint32()
         loop_ms = ctypes.c_double()
         total_ms = ctypes.c_double()

@@ -562,8 +562,21 @@ std::vector<uint32_t> resolve_outlets(const fl_graph* g, const uint8_t* is_outle
     std::vector<uint32_t> o;
     for (uint32_t t = 0; t < g->terrains; ++t) {
         const size_t first = o.size();
-        for (uint32_t i = g->site_off[t]; i < g->site_off[t + 1]; ++i)
+        const uint32_t end = g->site_off[t + 1];
+        uint32_t i = g->site_off[t];
+        while (i < end) {
+            // outlets are sparse: step over eight zero flags at a time
+            if (i + 8 <= end) {
+                uint64_t word;
+                std::memcpy(&word, is_outlet + i, 8);
+                if (word == 0) {
+                    i += 8;
+                    continue;
+                }
+            }
             if (is_outlet[i]) o.push_back(g->inv[i]);
+            ++i;
+        }
         if (o.size() == first)
             o.insert(o.end(), g->def_outlets.begin() + g->def_off[t],
                      g->def_outlets.begin() + g->def_off[t + 1]);
@@ -885,8 +898,10 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     FL_CU(cudaSetDevice(g->device));
     auto t_start = std::chrono::steady_clock::now();
     uint32_t n = g->n;
-    std::vector<uint32_t> outlets = resolve_outlets(g, is_outlet);
+    // the uploads are asynchronous from page-locked memory: scan the outlet flags on the
+    // host meanwhile
     FL_TRY(upload_params(g, base, k, u, max_slope));
+    std::vector<uint32_t> outlets = resolve_outlets(g, is_outlet);
     FL_TRY(set_outlets(g, outlets, false));
     // all status words, including the grid barrier's, start from zero
     FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
@@ -1150,6 +1165,23 @@ int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
 }
 
 void fl_graph_destroy(fl_graph* g) { free_graph(g); }
+
+int fl_host_alloc(uint64_t bytes, void** out) {
+    g_err.clear();
+    if (!out || bytes == 0) return FL_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        set_err("cudaHostAlloc", e);
+        *out = nullptr;
+        return e == cudaErrorMemoryAllocation ? FL_ERR_OUT_OF_MEMORY : FL_ERR_CUDA;
+    }
+    return FL_OK;
+}
+
+void fl_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
 
 uint32_t fl_graph_num_sites(const fl_graph* g) { return g ? g->n : 0; }
 uint64_t fl_graph_num_slots(const fl_graph* g) { return g ? g->nnz : 0; }

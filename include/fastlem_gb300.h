@@ -90,6 +90,14 @@ int fl_generate_timed(fl_graph* g, uint32_t n_params, const double* base,
                       const double* max_slope, int64_t max_iteration, double* out_elev,
                       uint32_t* out_iterations, double* loop_ms, double* total_ms);
 
+/* Page-locked host memory (no fastlem counterpart).  Parameter and output arrays in
+ * such memory move between host and device by DMA at the link's rate and let the
+ * parameter uploads overlap the host-side outlet scan; fl_generate accepts any host
+ * memory.  fl_host_alloc(0, ...) -> FL_ERR_INVALID_ARGUMENT; fl_host_free(NULL) is
+ * ignored. */
+int fl_host_alloc(uint64_t bytes, void** out);
+void fl_host_free(void* p);
+
 /* Number of vertices / adjacency slots of a model. */
 uint32_t fl_graph_num_sites(const fl_graph* g);
 uint64_t fl_graph_num_slots(const fl_graph* g);

@@ -241,6 +241,28 @@ def test_generate_small_config_with_max_slope(orc):
     _parity_run(orc, workloads.small(max_slope=0.314))
 
 
+@pytest.mark.parametrize("max_slope", [None, 0.314])
+def test_pinned_host_buffers_give_the_same_result(max_slope):
+    """Parameters in page-locked memory (ParameterArrays.pinned) and a reused pinned
+    output array give the bits of the pageable path, call after call."""
+    from fastlem_gb300 import pinned_empty
+    w = workloads.small(scale=0.5, max_slope=max_slope)
+    m, p = w.model, w.params
+    want = TerrainGenerator.default().set_model(m).set_parameters(p).set_max_iteration(12)
+    want = want.generate().elevations()
+    pp = p.pinned()
+    assert all(np.array_equal(getattr(pp, k), getattr(p, k), equal_nan=True)
+               for k in ("base", "erodibility", "uplift", "is_outlet"))
+    out = pinned_empty(m.num(), np.float64)
+    gen = TerrainGenerator.default().set_model(m).set_parameters(pp).set_max_iteration(12)
+    for _ in range(2):
+        out[:] = np.nan
+        got = gen.generate(out=out).elevations()
+        assert_bits_equal(got, want, "pinned")
+        assert_bits_equal(out, want, "pinned out buffer")
+    m.release()
+
+
 def test_generate_reference_landscape_evolution_test(orc):
     """The setup of fastlem's tests/landscape_evolution.rs:9-34: 10,000 random sites in
     [0,200]x[0,100], one relaxation, all default parameters but max_slope 3.14*0.1, no
