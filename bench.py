@@ -41,7 +41,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="16m", choices=["small", "1m", "16m", "batched", "served"])
     ap.add_argument("--requests", type=int, default=64, help="served: requests in the stream")
-    ap.add_argument("--slots", type=int, default=4, help="served: concurrent requests")
+    ap.add_argument("--slots", type=int, default=12, help="served: concurrent requests (worker threads)")
     ap.add_argument("--serve-iters", type=int, default=64,
                     help="served: set_max_iteration per request (fastlem's loop may not settle)")
     ap.add_argument("--terrains", type=int, default=512, help="batched: terrain count")
@@ -154,16 +154,25 @@ def peak_hbm():
 
 # DRAM bytes (read + write) of one launch from an ncu capture, per unit the kernel
 # processes; a capture of the full 16M workload does not fit the profiling size rule,
-# so the 1M config's launch is scaled by the units (traffic grows with them).
+# so the 1M config's launch (8th iteration of a generate(), --set full) is scaled by
+# the units (traffic grows with them).
 NCU_TRAFFIC = {
-    # profiles/k_kahn_1m.md: 52.80 MB for the 921,868 Kahn-region sites of the 1M config
-    "kahn_rounds": (52.80e6 / 921_868, "kahn_sites",
+    # 52.31 MB over the 891,787 Kahn-region sites (1,000,000 - 108,213 skeleton sites)
+    "kahn_rounds": (52.306e6 / 891_787, "kahn_sites",
                     "ncu dram__bytes_read+write of one k_kahn launch on the 1M config "
-                    "(profiles/k_kahn_1m.md), scaled by Kahn-region sites"),
-    # profiles/k_s_bottom_up_1m.md: 4.31 MB for 78,132 skeleton sites
-    "skeleton_up": (4.31e6 / 78_132, "skeleton_sites",
+                    "(8th iteration), scaled by Kahn-region sites"),
+    # 6.421 MB over 108,213 skeleton sites
+    "skeleton_up": (6.421e6 / 108_213, "skeleton_sites",
                     "ncu dram__bytes_read+write of one k_s_bottom_up launch on the 1M config "
-                    "(profiles/k_s_bottom_up_1m.md), scaled by skeleton sites"),
+                    "(8th iteration), scaled by skeleton sites"),
+    # 113.20 MB over 1,000,000 sites
+    "receivers": (113.20e6 / 1_000_000, "sites",
+                  "ncu dram__bytes_read+write of one k_receivers launch on the 1M config "
+                  "(8th iteration), scaled by sites"),
+    # 39.41 MB over 1,000,000 sites
+    "response_w": (39.41e6 / 1_000_000, "sites",
+                   "ncu dram__bytes_read+write of one k_w launch on the 1M config "
+                   "(8th iteration), scaled by sites"),
 }
 
 
@@ -171,7 +180,8 @@ def measured_traffic(kernel, basin, n):
     if kernel not in NCU_TRAFFIC:
         return None, "no ncu capture for this kernel"
     per, unit, src = NCU_TRAFFIC[kernel]
-    units = basin["skeleton_sites"] if unit == "skeleton_sites" else n - basin["skeleton_sites"]
+    units = {"skeleton_sites": basin["skeleton_sites"], "sites": n,
+             "kahn_sites": n - basin["skeleton_sites"]}[unit]
     return per * units, src
 
 
