@@ -203,6 +203,46 @@ def run_cpu_sample(w, iters):
     return w.model.num() * r["iters"] / r["seconds"], r["iters"], r["seconds"]
 
 
+def cpu_pool_sample(models, params, iters, per_terrain_iters, budget_s=12.0):
+    """All host cores on independent terrains: the oracle in a thread pool (its C calls
+    release the GIL), on terrains spread over the workload's sizes (every k-th by size),
+    each bounded to min(iters, what one core does in about budget_s).  Returns
+    (aggregate site-iterations per second, threads, description); the workload's
+    terrains/s on the host is that rate over `per_terrain_iters` (the mean
+    site-iterations of one of its terrains, from the GPU run)."""
+    import concurrent.futures as cf
+    import threading
+    from oracle import oracle as orc
+    from tests import graphs
+    threads = os.cpu_count() or 1
+    order = np.argsort([m.num() for m in models], kind="stable")
+    k = min(len(order), 4 * threads)
+    pick = order[np.linspace(0, len(order) - 1, k).round().astype(int)]
+    per_core = 0.6e6 * budget_s                          # site-iterations a core does
+    done = []
+    lock = threading.Lock()
+
+    def one(i):
+        m, p = models[i], params[i]
+        mi = int(max(1, min(iters, per_core // m.num())))
+        r = orc.generate(graphs.from_model(m), p.base, p.erodibility, p.uplift, p.is_outlet,
+                         max_slope=p.max_slope, max_iter=mi)
+        with lock:
+            done.append(m.num() * r["iters"])
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one, pick))
+    secs = time.perf_counter() - t0
+    rate = sum(done) / secs
+    desc = (f"oracle generate() on {len(pick)} of the {len(models)} terrains (every k-th by "
+            f"size, {min(m.num() for m in models):,}-{max(m.num() for m in models):,} sites), "
+            f"each bounded to <= {iters} iterations and ~{int(per_core):,} site-iterations, "
+            f"{threads} threads, {secs:.1f} s; terrains/s = site-iterations/s over the mean "
+            f"{per_terrain_iters:,.0f} site-iterations of a terrain in the GPU run")
+    return rate, threads, desc
+
+
 def workload_name(w):
     c = w.config
     return (f"{w.name}: {c['sites']:,} sites uniform in [0,{c['box']:g}]^2 seed {c['seed']}, "
@@ -295,6 +335,11 @@ def bench_gpu(args, d):
     all_bytes = sum(v[2] for v in stats.values())
     all_ms = sum(v[1] for v in stats.values())
     traffic, traffic_src = measured_traffic(dname, basin, n)
+    # the whole solve against the per-site-iteration byte count of the path: per-site
+    # inputs 37 B, 12 B per slot, intermediates 48 B, output 8 B
+    dbar = float(m.row_ptr[-1]) / n
+    b_alg = 93.0 + 12.0 * dbar
+    whole = b_alg * site_iters / (loop_max / 1000) / 1e9
     roof = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
             "traffic_source": traffic_src,
@@ -304,7 +349,10 @@ def bench_gpu(args, d):
             # device time
             "all_kernels": {"achieved": all_bytes / (all_ms / 1000) / 1e9 if all_ms else 0.0,
                             "frac": (all_bytes / (all_ms / 1000) / 1e9 / peak) if all_ms else 0.0,
-                            "bytes_per_iteration": all_bytes / max(1, iters)}}
+                            "bytes_per_iteration": all_bytes / max(1, iters)},
+            # (93 + 12 d) B per site-iteration over the loop's device time
+            "whole_solve": {"bytes_per_site_iteration": b_alg, "mean_degree": dbar,
+                            "achieved": whole, "frac": whole / peak}}
     share = {k: round(v[1] / max(1e-9, sum(x[1] for x in stats.values())), 4)
              for k, v in stats.items() if v[0]}
     cpu = None
@@ -345,12 +393,13 @@ def bench_gpu(args, d):
         ea.steps, ea.warmup, ea.batch_iters, ea.requests, ea.serve_iters = 2, 1, 64, 32, 64
         b = bench_batched(ea, d, emit=False)
         line["batched"] = {k: b[k] for k in ("metric", "value", "unit", "e2e", "plain_loop",
-                                              "speedup_vs_plain_loop", "identical_to_plain")}
+                                              "speedup_vs_plain_loop", "identical_to_plain",
+                                              "cpu_baseline")}
         line["batched"]["config"] = b["config"]
         sv = bench_served(ea, d, emit=False)
         line["served"] = {k: sv[k] for k in ("metric", "value", "unit", "latency_ms",
                                               "sequential_plain", "speedup_vs_sequential",
-                                              "identical_to_plain", "server")}
+                                              "identical_to_plain", "cpu_baseline", "server")}
         line["served"]["config"] = sv["config"]
     print(json.dumps(line), flush=True)
 
@@ -411,6 +460,11 @@ def bench_batched(args, d, emit=True):
     plain_tps = count / (plain_loop_ms / 1000)
     plain_tps_wall = count / plain_wall
     h2d = sites * (8 + 8 + 8 + 1)
+    cpu = None
+    if not args.no_cpu_baseline and args.gpus == 1:
+        rate, thr, desc = cpu_pool_sample(w.models, w.params, args.batch_iters, site_iters / count)
+        cpu = {"value": rate / (site_iters / count), "unit": "terrains/s", "cores": thr,
+               "kind": "port", "site_iterations_per_s": rate, "sample": desc}
     line = {
         "metric": "batched terrains/s (512 terrains, 4,096-262,144 sites)",
         "value": value, "unit": "terrains/s", "n_gpus": args.gpus, "steps": args.steps,
@@ -435,6 +489,7 @@ def bench_batched(args, d, emit=True):
         "speedup_vs_plain_loop": value / plain_tps,
         "speedup_vs_plain_loop_wall": (count * args.steps / wall) / plain_tps_wall,
         "identical_to_plain": identical,
+        "cpu_baseline": cpu,
         "clocks": clocks.summary(),
     }
     if emit:
@@ -496,6 +551,11 @@ def bench_served(args, d, emit=True):
     iters = np.array([info["iterations"] for _, info in served])
     site_iters = int(sum(m.num() * int(i) for m, i in zip(w.models, iters)))
     value = R / span
+    cpu = None
+    if not args.no_cpu_baseline and args.gpus == 1:
+        rate, thr, desc = cpu_pool_sample(w.models, w.params, cap, site_iters / R)
+        cpu = {"value": rate / (site_iters / R), "unit": "terrains/s", "cores": thr,
+               "kind": "port", "site_iterations_per_s": rate, "sample": desc}
     line = {
         "metric": "served terrains/s and p99 latency (Poisson 200 req/s, 16,384-4,194,304 sites)",
         "value": value, "unit": "terrains/s", "n_gpus": args.gpus, "steps": 1, "warmup": 1,
@@ -518,6 +578,7 @@ def bench_served(args, d, emit=True):
                                             "p99": float(np.percentile(seq_lat, 99))}},
         "speedup_vs_sequential": (R / span) / (R / seq_span),
         "identical_to_plain": identical,
+        "cpu_baseline": cpu,
         "server": stats,
         "clocks": clocks.summary(),
     }
