@@ -1168,8 +1168,8 @@ void fl_graph_destroy(fl_graph* g) { free_graph(g); }
 
 int fl_host_alloc(uint64_t bytes, void** out) {
     g_err.clear();
+    if (out) *out = nullptr;
     if (!out || bytes == 0) return FL_ERR_INVALID_ARGUMENT;
-    *out = nullptr;
     cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
     if (e != cudaSuccess) {
         set_err("cudaHostAlloc", e);

@@ -93,8 +93,8 @@ int fl_generate_timed(fl_graph* g, uint32_t n_params, const double* base,
 /* Page-locked host memory (no fastlem counterpart).  Parameter and output arrays in
  * such memory move between host and device by DMA at the link's rate and let the
  * parameter uploads overlap the host-side outlet scan; fl_generate accepts any host
- * memory.  fl_host_alloc(0, ...) -> FL_ERR_INVALID_ARGUMENT; fl_host_free(NULL) is
- * ignored. */
+ * memory.  *out is NULL after any failure; fl_host_alloc(0, ...) ->
+ * FL_ERR_INVALID_ARGUMENT; fl_host_free(NULL) is ignored. */
 int fl_host_alloc(uint64_t bytes, void** out);
 void fl_host_free(void* p);
 

@@ -127,3 +127,34 @@ def test_server_host_checks(fl_lib):
         assert fl_lib.fl_server_wait(s, 12345, None, None, None, None) == FL_ERR_INVALID_ARGUMENT
     finally:
         fl_lib.fl_server_destroy(s)
+
+
+def test_host_alloc_argument_checks(fl_lib):
+    """fl_host_alloc rejects a zero size or a missing out pointer before any CUDA call;
+    fl_host_free ignores NULL."""
+    from fastlem_gb300._lib import FL_ERR_INVALID_ARGUMENT
+    p = ctypes.c_void_p(1234)
+    assert fl_lib.fl_host_alloc(0, ctypes.byref(p)) == FL_ERR_INVALID_ARGUMENT
+    assert p.value is None
+    assert fl_lib.fl_host_alloc(64, None) == FL_ERR_INVALID_ARGUMENT
+    fl_lib.fl_host_free(None)
+
+
+def test_model_device_bytes_bound_grows_with_the_model(fl_lib):
+    """The admission bound covers the per-site and per-slot arrays of a model."""
+    b1 = fl_lib.fl_model_device_bytes(1000, 6000)
+    b2 = fl_lib.fl_model_device_bytes(2000, 12000)
+    assert b2 > b1 >= 1000 * 360 + 6000 * 16
+    assert fl_lib.fl_model_device_bytes(1000, 7000) - b1 == 1000 * 16
+
+
+def test_generate_rejects_a_bad_output_buffer():
+    """generate(out=...) wants a contiguous float64 array of num() sites."""
+    import math
+    from fastlem_gb300 import workloads
+    w = workloads.small(scale=0.01)
+    gen = TerrainGenerator.default().set_model(w.model).set_parameters(w.params)
+    for bad in (np.empty(w.model.num(), np.float32), np.empty(w.model.num() + 1),
+                np.empty(2 * w.model.num())[::2]):
+        with pytest.raises(ValueError):
+            gen.generate(out=bad)
