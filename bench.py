@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--iters", type=int, default=8, help="set_max_iteration per step")
     ap.add_argument("--cpu-iters", type=int, default=1, help="iterations in the CPU sample")
+    ap.add_argument("--cpu-threads", type=int, default=0,
+                    help="reference arm: replica threads (0: every core the memory allows)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="16M run: skip the batched (C4) and served (C5) summaries")
@@ -249,32 +251,62 @@ def workload_name(w):
             f"relax {c['relax']}, outlets {c['outlets']}, erodibility {c['erodibility']}")
 
 
+def host_replica_threads(n):
+    """Replica threads the host can run for an n-site model: every core, bounded by the
+    available memory (about 250 B per site for one oracle solve's state)."""
+    cores = os.cpu_count() or 1
+    try:
+        with open("/proc/meminfo") as f:
+            avail = next(int(l.split()[1]) * 1024 for l in f if l.startswith("MemAvailable:"))
+    except (OSError, StopIteration, ValueError):
+        return 1
+    return max(1, min(cores, int(avail * 0.6 // (250 * max(1, n)))))
+
+
 def bench_reference(args, d):
+    """The reference's path on the host cores: fastlem's generate() is single-threaded,
+    so all cores run independent replicas of the same solve (one per thread; the
+    oracle's C calls release the GIL), each bounded to --cpu-iters iterations per step.
+    value = site-iterations of all replicas / wall time of the step."""
     if d.rank != 0:
         return
+    import concurrent.futures as cf
     from oracle import build as ob
+    from oracle import oracle as orc
+    from tests import graphs
     ob.build()
+    orc.lib()
     w, build_s = make_workload(args)
     n = w.model.num()
-    for _ in range(args.warmup):
-        run_cpu_sample(w, args.cpu_iters)
-    vals, secs, its = [], 0.0, 0
-    for _ in range(args.steps):
-        v, it, s = run_cpu_sample(w, args.cpu_iters)
-        vals.append(v)
-        secs += s
-        its += it
+    g = graphs.from_model(w.model)
+    p = w.params
+    threads = args.cpu_threads or host_replica_threads(n)
+
+    def solve(_):
+        r = orc.generate(g, p.base, p.erodibility, p.uplift, p.is_outlet,
+                         max_slope=p.max_slope, max_iter=args.cpu_iters)
+        return r["iters"]
+
+    secs, its = 0.0, 0
+    with cf.ThreadPoolExecutor(threads) as ex:
+        for _ in range(args.warmup):
+            list(ex.map(solve, range(threads)))
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            its += sum(ex.map(solve, range(threads)))
+            secs += time.perf_counter() - t0
     value = n * its / secs / 1e6
-    sample = (f"generate() with set_max_iteration({args.cpu_iters}) per step on the same "
-              f"{n:,}-site model, 1 thread")
+    sample = (f"{threads} concurrent replicas (one thread each) of generate() with "
+              f"set_max_iteration({args.cpu_iters}) on the same {n:,}-site model per step")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Msite-iters/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(w), "iterations_per_step": args.cpu_iters},
-        "cpu_baseline": {"value": value, "unit": "Msite-iters/s", "cores": 1, "kind": "port",
-                         "sample": sample},
+        "config": {"workload": workload_name(w), "iterations_per_step": args.cpu_iters,
+                   "host_threads": threads, "host_cores": os.cpu_count()},
+        "cpu_baseline": {"value": value, "unit": "Msite-iters/s", "cores": threads,
+                         "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Msite-iters/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
