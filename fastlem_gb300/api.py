@@ -201,8 +201,15 @@ class TerrainModel2D:
         except Exception:
             pass
 
+    def interpolator(self):
+        """The sites' natural-neighbour interpolator (built on first use, host memory),
+        shared by every Terrain2D of this model (models/surface/model.rs:62-68)."""
+        if getattr(self, "_interp", None) is None:
+            self._interp = TerrainInterpolator2D(self.xs, self.ys)
+        return self._interp
+
     def create_terrain_from_result(self, elevations):
-        return Terrain2D(self.xs, self.ys, elevations)
+        return Terrain2D(self.xs, self.ys, elevations, interpolator=self.interpolator)
 
 
 class TerrainModel2DBulider:
@@ -329,13 +336,53 @@ class TerrainModel2DBulider:
                               hull[:nh.value].copy())
 
 
+class TerrainInterpolator2D:
+    """models/surface/interpolator.rs:6-29: Sibson natural-neighbour interpolation over
+    the sites' Delaunay triangulation (fl_interpolator_*); None outside the convex hull."""
+
+    def __init__(self, xs, ys):
+        self.xs, self.ys = as_f64(xs), as_f64(ys)
+        h = ctypes.c_void_p()
+        check(lib().fl_interpolator_create(len(self.xs), ptr(self.xs), ptr(self.ys),
+                                           ctypes.byref(h)))
+        self._h = h
+
+    def interpolate_many(self, elevations, qx, qy):
+        """(values, found) for arrays of query coordinates; values are NaN where the
+        query lies outside the hull (found False)."""
+        e = as_f64(elevations)
+        if len(e) != len(self.xs):
+            raise ValueError("one elevation per site")
+        qx, qy = as_f64(qx), as_f64(qy)
+        if qx.shape != qy.shape:
+            raise ValueError("qx and qy differ in shape")
+        out = np.empty(qx.shape, np.float64)
+        found = np.empty(qx.shape, np.uint8)
+        check(lib().fl_interpolate(self._h, ptr(e), qx.size, ptr(qx), ptr(qy), ptr(out),
+                                   ptr(found)))
+        return out, found.astype(bool)
+
+    def interpolate(self, elevations, site):
+        v, ok = self.interpolate_many(elevations, np.array([site.x]), np.array([site.y]))
+        return float(v[0]) if ok[0] else None
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None) is not None:
+                lib().fl_interpolator_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
 class Terrain2D:
     """models/surface/terrain.rs:8-39."""
 
-    def __init__(self, xs, ys, elevations):
+    def __init__(self, xs, ys, elevations, interpolator=None):
         self.xs = xs
         self.ys = ys
         self._elev = elevations
+        self._interp = interpolator      # a TerrainInterpolator2D or a callable making one
 
     def sites(self):
         return [Site2D(float(x), float(y)) for x, y in zip(self.xs, self.ys)]
@@ -343,9 +390,20 @@ class Terrain2D:
     def elevations(self):
         return self._elev
 
+    def _interpolator(self):
+        if self._interp is None:
+            self._interp = TerrainInterpolator2D(self.xs, self.ys)
+        elif not isinstance(self._interp, TerrainInterpolator2D):
+            self._interp = self._interp()
+        return self._interp
+
     def get_elevation(self, site: Site2D):
-        raise NotImplementedError(
-            "natural-neighbour interpolation (interpolator.rs) is not part of the GB300 solve")
+        """Interpolated elevation at `site` (terrain.rs:35-38), None outside the hull."""
+        return self._interpolator().interpolate(self._elev, site)
+
+    def get_elevations(self, xs, ys):
+        """get_elevation for arrays of coordinates at once: NaN where it is None."""
+        return self._interpolator().interpolate_many(self._elev, xs, ys)[0]
 
 
 class TerrainGenerator:

@@ -28,6 +28,7 @@
 #include <thread>
 #include <vector>
 
+#include "delaunay.h"
 #include "fastlem_gb300.h"
 #include "rng.h"
 
@@ -522,6 +523,25 @@ void voronoi_cells(const SweepHull& d, double x0, double y0, double x1, double y
 }
 
 }  // namespace
+
+bool delaunay(uint32_t n, const double* xs, const double* ys, std::vector<uint32_t>& tri,
+              std::vector<int64_t>& half) {
+    SweepHull d{xs, ys, n};
+    if (!d.run()) return false;
+    tri = std::move(d.tri);
+    half = std::move(d.half);
+    return true;
+}
+
+double orient2d(double ax, double ay, double bx, double by, double cx, double cy) {
+    return orient(ax, ay, bx, by, cx, cy);
+}
+
+double incircle2d(double ax, double ay, double bx, double by, double cx, double cy, double dx,
+                  double dy) {
+    return incircle(ax, ay, bx, by, cx, cy, dx, dy);
+}
+
 }  // namespace fl
 
 // ---------------------------------------------------------------------------

@@ -290,6 +290,22 @@ int fl_build_graph(uint32_t n, const double* xs, const double* ys, double x0, do
 int64_t fl_triangulate(uint32_t n, const double* xs, const double* ys, uint32_t* tri,
                        uint64_t cap);
 
+/* ---- Terrain2D::get_elevation (models/surface/terrain.rs:35-38) ----
+ *
+ * `TerrainInterpolator2D::new(sites)` (models/surface/interpolator.rs:10-15) and its
+ * `interpolate(elevations, site)` (interpolator.rs:17-29): Sibson natural-neighbour
+ * interpolation, None outside the sites' convex hull.  fl_interpolate answers `count`
+ * queries at once: out[i] = the interpolated value and found[i] = 1, or out[i] = NaN
+ * and found[i] = 0 (the reference's None).  A query on a hull edge takes the linear
+ * interpolant along it; a query equal to a site returns its value.  Host computation,
+ * threads for large batches.
+ *   fewer than three sites / all collinear / a non-finite site -> FL_ERR_INVALID_ARGUMENT */
+typedef struct fl_interpolator fl_interpolator;
+int fl_interpolator_create(uint32_t n, const double* xs, const double* ys, fl_interpolator** out);
+void fl_interpolator_destroy(fl_interpolator* it);
+int fl_interpolate(const fl_interpolator* it, const double* values, uint64_t count,
+                   const double* qx, const double* qy, double* out, uint8_t* found);
+
 #ifdef __cplusplus
 }
 #endif
