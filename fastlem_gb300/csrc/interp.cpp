@@ -257,8 +257,26 @@ int fl_interpolate(const fl_interpolator* it, const double* values, uint64_t cou
         fl::set_last_error("fl_interpolate: null argument");
         return FL_ERR_INVALID_ARGUMENT;
     }
+    // large batches run in grid-cell order (a counting sort of the queries), so that
+    // neighbouring queries walk the same triangles; every query is independent
+    std::vector<uint64_t> order;
+    if (count >= 4096) {
+        const uint64_t cells = (uint64_t)it->gw * it->gh;
+        std::vector<uint64_t> cell(count), start(cells + 1, 0);
+        for (uint64_t i = 0; i < count; ++i) {
+            const double fx = (qx[i] - it->gx0) / it->gsx, fy = (qy[i] - it->gy0) / it->gsy;
+            const uint64_t cx = fx > 0 ? (uint64_t)std::min<double>(it->gw - 1, fx) : 0;
+            const uint64_t cy = fy > 0 ? (uint64_t)std::min<double>(it->gh - 1, fy) : 0;
+            cell[i] = cy * it->gw + cx;
+            ++start[cell[i] + 1];
+        }
+        for (uint64_t c = 0; c < cells; ++c) start[c + 1] += start[c];
+        order.resize(count);
+        for (uint64_t i = 0; i < count; ++i) order[start[cell[i]]++] = i;
+    }
     auto run = [&](uint64_t a, uint64_t b) {
-        for (uint64_t i = a; i < b; ++i) {
+        for (uint64_t k = a; k < b; ++k) {
+            const uint64_t i = order.empty() ? k : order[k];
             double v = NAN;
             found[i] = interpolate_one(*it, values, qx[i], qy[i], &v) ? 1 : 0;
             out[i] = found[i] ? v : NAN;
