@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <thread>
 #include <vector>
 
 namespace fl {
@@ -36,6 +37,29 @@ static uint64_t hilbert_index(uint32_t order, uint32_t x, uint32_t y) {
     return d;
 }
 
+// Threads for a host pass over `work` items: all cores for large passes.
+static unsigned host_threads(uint64_t work) {
+    unsigned t = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    return work < (1u << 18) ? 1u : t;
+}
+
+// Runs f(a, b) over [0, n) split into `nt` contiguous ranges on as many threads.
+template <class F>
+static void parallel_ranges(uint64_t n, unsigned nt, F f) {
+    if (nt <= 1) {
+        f((uint64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const uint64_t chunk = (n + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; ++t) {
+        const uint64_t a = std::min<uint64_t>((uint64_t)t * chunk, n);
+        const uint64_t b = std::min<uint64_t>(a + chunk, n);
+        if (a < b) th.emplace_back(f, a, b);
+    }
+    for (auto& x : th) x.join();
+}
+
 // perm[new] = old for the Hilbert order of (xs, ys); ties keep index order.
 void hilbert_order(uint32_t n, const double* xs, const double* ys, std::vector<uint32_t>& perm) {
     double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
@@ -47,25 +71,27 @@ void hilbert_order(uint32_t n, const double* xs, const double* ys, std::vector<u
     const double cells = (double)((1u << order) - 1);
     double sx = (x1 > x0) ? cells / (x1 - x0) : 0.0;
     double sy = (y1 > y0) ? cells / (y1 - y0) : 0.0;
-    std::vector<uint32_t> key(n);
-    for (uint32_t i = 0; i < n; ++i) {
-        double fx = std::isfinite(xs[i]) ? (xs[i] - x0) * sx : 0.0;
-        double fy = std::isfinite(ys[i]) ? (ys[i] - y0) * sy : 0.0;
-        uint32_t cx = (uint32_t)std::min(cells, std::max(0.0, fx));
-        uint32_t cy = (uint32_t)std::min(cells, std::max(0.0, fy));
-        key[i] = (uint32_t)hilbert_index(order, cx, cy);   // < 2^32 for order 16
+    // (key << 32 | index): an LSD radix sort on the key bytes keeps index order on ties
+    std::vector<uint64_t> a(n), b(n);
+    parallel_ranges(n, host_threads(n), [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            double fx = std::isfinite(xs[i]) ? (xs[i] - x0) * sx : 0.0;
+            double fy = std::isfinite(ys[i]) ? (ys[i] - y0) * sy : 0.0;
+            uint32_t cx = (uint32_t)std::min(cells, std::max(0.0, fx));
+            uint32_t cy = (uint32_t)std::min(cells, std::max(0.0, fy));
+            const uint64_t key = hilbert_index(order, cx, cy);   // < 2^32 for order 16
+            a[i] = (key << 32) | i;
+        }
+    });
+    for (int shift = 32; shift < 64; shift += 8) {
+        uint64_t cnt[257] = {0};
+        for (uint32_t i = 0; i < n; ++i) ++cnt[((a[i] >> shift) & 255u) + 1];
+        for (int k = 0; k < 256; ++k) cnt[k + 1] += cnt[k];
+        for (uint32_t i = 0; i < n; ++i) b[cnt[(a[i] >> shift) & 255u]++] = a[i];
+        a.swap(b);
     }
-    // stable LSD radix sort of (key, index), 4 passes of 8 bits
     perm.resize(n);
-    for (uint32_t i = 0; i < n; ++i) perm[i] = i;
-    std::vector<uint32_t> tmp(n);
-    for (int shift = 0; shift < 32; shift += 8) {
-        uint32_t cnt[257] = {0};
-        for (uint32_t i = 0; i < n; ++i) ++cnt[((key[perm[i]] >> shift) & 255u) + 1];
-        for (int b = 0; b < 256; ++b) cnt[b + 1] += cnt[b];
-        for (uint32_t i = 0; i < n; ++i) tmp[cnt[(key[perm[i]] >> shift) & 255u]++] = perm[i];
-        perm.swap(tmp);
-    }
+    for (uint32_t i = 0; i < n; ++i) perm[i] = (uint32_t)a[i];
 }
 
 // CSR of the relabelled graph: new row j is old row perm[j] with columns mapped
@@ -77,14 +103,16 @@ void relabel_csr(uint32_t n, const uint32_t* row, const uint32_t* col, const dou
     for (uint32_t j = 0; j < n; ++j) nrow[j + 1] = nrow[j] + (row[perm[j] + 1] - row[perm[j]]);
     ncol.resize(nrow[n]);
     nlen.resize(nrow[n]);
-    for (uint32_t j = 0; j < n; ++j) {
-        uint32_t o = perm[j];
-        uint32_t d = nrow[j];
-        for (uint32_t s = row[o]; s < row[o + 1]; ++s, ++d) {
-            ncol[d] = inv[col[s]];
-            nlen[d] = len[s];
+    parallel_ranges(n, host_threads(nrow[n]), [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t j = lo; j < hi; ++j) {
+            const uint32_t o = perm[j];
+            uint32_t d = nrow[j];
+            for (uint32_t s = row[o]; s < row[o + 1]; ++s, ++d) {
+                ncol[d] = inv[col[s]];
+                nlen[d] = len[s];
+            }
         }
-    }
+    });
 }
 
 }  // namespace fl

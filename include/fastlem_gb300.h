@@ -286,6 +286,15 @@ int fl_build_graph(uint32_t n, const double* xs, const double* ys, double x0, do
                    uint64_t cap, double* area, uint32_t* hull, uint64_t* out_nnz,
                    uint32_t* out_nhull);
 
+/* The lake-heap processing order of remove_lakes_from_stream_tree
+ * (lem/stream_tree.rs:175-243): rank[v] = the position at which the heap traversal
+ * from `outlets` (pushed in order with key 0) processes site v, UINT32_MAX if never.
+ * It depends only on the graph, the lengths and the outlet list (the solver computes
+ * it once per model and outlet list).  Host computation.
+ *   an out-of-range id or a NaN length met by the traversal -> FL_ERR_INVALID_ARGUMENT */
+int fl_lake_rank(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
+                 const uint32_t* outlets, uint32_t n_out, uint32_t* rank);
+
 /* Raw triangulation (counter-clockwise triangles); returns the triangle count. */
 int64_t fl_triangulate(uint32_t n, const double* xs, const double* ys, uint32_t* tri,
                        uint64_t cap);
