@@ -25,6 +25,7 @@
 #include <cstdint>
 #include <cstring>
 #include <numeric>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -515,9 +516,14 @@ void voronoi_cells(const SweepHull& d, double x0, double y0, double x1, double y
     for (unsigned t = 0; t < nt; ++t) {
         uint32_t a = std::min<uint64_t>((uint64_t)t * chunk, n);
         uint32_t b = std::min<uint64_t>((uint64_t)a + chunk, n);
-        th.emplace_back([&, a, b] {
+        auto cells = [&, a, b] {
             voronoi_cells_range(d, ccx, ccy, start, hullv, x0, y0, x1, y1, a, b, area, cenx, ceny);
-        });
+        };
+        try {
+            th.emplace_back(cells);
+        } catch (const std::system_error&) {   // no thread to spare: run it here
+            cells();
+        }
     }
     for (auto& t : th) t.join();
 }

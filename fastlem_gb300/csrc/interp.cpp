@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -288,7 +289,12 @@ int fl_interpolate(const fl_interpolator* it, const double* values, uint64_t cou
     const uint64_t chunk = (count + nt - 1) / nt;
     for (unsigned t = 0; t < nt; ++t) {
         const uint64_t a = std::min<uint64_t>(t * chunk, count), b = std::min<uint64_t>(a + chunk, count);
-        if (a < b) th.emplace_back(run, a, b);
+        if (a >= b) continue;
+        try {
+            th.emplace_back(run, a, b);
+        } catch (const std::system_error&) {   // no thread to spare: run it here
+            run(a, b);
+        }
     }
     for (auto& t : th) t.join();
     return FL_OK;

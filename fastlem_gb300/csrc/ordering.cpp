@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -55,7 +56,12 @@ static void parallel_ranges(uint64_t n, unsigned nt, F f) {
     for (unsigned t = 0; t < nt; ++t) {
         const uint64_t a = std::min<uint64_t>((uint64_t)t * chunk, n);
         const uint64_t b = std::min<uint64_t>(a + chunk, n);
-        if (a < b) th.emplace_back(f, a, b);
+        if (a >= b) continue;
+        try {
+            th.emplace_back(f, a, b);
+        } catch (const std::system_error&) {   // no thread to spare: run it here
+            f(a, b);
+        }
     }
     for (auto& x : th) x.join();
 }

@@ -25,6 +25,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -218,7 +219,13 @@ int fl_server_create(uint64_t hbm_budget_bytes, uint32_t slots, fl_server** out)
     s->budget = hbm_budget_bytes;
     s->slots = slots;
     if (cudaGetDevice(&s->device) != cudaSuccess) s->device = 0;
-    for (uint32_t i = 0; i < slots; ++i) s->workers.emplace_back(worker, s);
+    try {
+        for (uint32_t i = 0; i < slots; ++i) s->workers.emplace_back(worker, s);
+    } catch (const std::system_error&) {
+        fl_server_destroy(s);                  // stops and joins the workers started
+        fl::set_last_error("fl_server_create: cannot start the worker threads");
+        return FL_ERR_OUT_OF_MEMORY;
+    }
     *out = s;
     return FL_OK;
 }
