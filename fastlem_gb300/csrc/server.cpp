@@ -234,7 +234,8 @@ int fl_server_add_model(fl_server* s, uint32_t n, const uint32_t* row_ptr, const
                         const double* len, const double* area, const uint32_t* default_outlets,
                         uint32_t n_default, const double* xs, const double* ys,
                         uint32_t* model_id) {
-    if (!s || !row_ptr || !area || !model_id || n == 0 || (n_default && !default_outlets)) {
+    if (!s || !row_ptr || !area || !model_id || n == 0 || (n_default && !default_outlets) ||
+        (row_ptr[n] && (!col || !len))) {
         fl::set_last_error("fl_server_add_model: invalid arguments");
         return FL_ERR_INVALID_ARGUMENT;
     }

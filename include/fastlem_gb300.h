@@ -152,7 +152,8 @@ typedef struct fl_server fl_server;
 
 int fl_server_create(uint64_t hbm_budget_bytes, uint32_t slots, fl_server** out);
 
-/* Registers a model (arguments as fl_graph_create; the arrays are copied). */
+/* Registers a model (arguments as fl_graph_create; the arrays are copied).  The graph
+ * itself is checked when a request first creates an instance of it. */
 int fl_server_add_model(fl_server* s, uint32_t n, const uint32_t* row_ptr, const uint32_t* col,
                         const double* len, const double* area, const uint32_t* default_outlets,
                         uint32_t n_default, const double* xs, const double* ys,
@@ -178,7 +179,8 @@ int fl_server_wait(fl_server* s, uint64_t ticket, uint32_t* out_iterations, doub
 int fl_server_stats(fl_server* s, uint64_t* out, uint32_t cap);
 
 /* Stops the workers after the requests they are running; waiting requests are
- * dropped.  Frees every instance. */
+ * dropped (their out_elev is never written).  Frees every instance and the server:
+ * no other fl_server_* call on `s` may run during or after it. */
 void fl_server_destroy(fl_server* s);
 
 /* Message for the last error on this thread ("" when none). */

@@ -113,6 +113,13 @@ def test_server_host_checks(fl_lib):
         area = np.ones(2)
         defs = np.array([0], np.uint32)
         mid = ctypes.c_uint32()
+        # adjacency slots without their columns or lengths
+        assert fl_lib.fl_server_add_model(s, 2, ptr(row_ptr), None, ptr(length), ptr(area),
+                                          ptr(defs), 1, None, None,
+                                          ctypes.byref(mid)) == FL_ERR_INVALID_ARGUMENT
+        assert fl_lib.fl_server_add_model(s, 2, ptr(row_ptr), ptr(col), None, ptr(area),
+                                          ptr(defs), 1, None, None,
+                                          ctypes.byref(mid)) == FL_ERR_INVALID_ARGUMENT
         assert fl_lib.fl_server_add_model(s, 2, ptr(row_ptr), ptr(col), ptr(length), ptr(area),
                                           ptr(defs), 1, None, None, ctypes.byref(mid)) == 0
         z, o = np.zeros(2), np.ones(2)
