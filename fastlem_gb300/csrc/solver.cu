@@ -985,7 +985,7 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
                  const double* xs, const double* ys, uint32_t k_terr, const uint32_t* site_off,
                  const uint32_t* def_off, fl_graph** out) {
     g_err.clear();
-    if (!out || !row_ptr || (!col && n) || !area || (n_default && !default_outlets) || n == 0 ||
+    if (!out || !row_ptr || (!col && n) || (!len && n) || !area || (n_default && !default_outlets) || n == 0 ||
         n >= kNone || k_terr == 0 || (k_terr > 1 && (!site_off || !def_off))) {
         g_err = "invalid graph arguments";
         return FL_ERR_INVALID_ARGUMENT;

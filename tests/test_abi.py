@@ -165,3 +165,17 @@ def test_generate_rejects_a_bad_output_buffer():
                 np.empty(2 * w.model.num())[::2]):
         with pytest.raises(ValueError):
             gen.generate(out=bad)
+
+
+def test_graph_create_rejects_missing_arrays(fl_lib):
+    """Null columns or lengths are rejected before anything is read or allocated."""
+    from fastlem_gb300._lib import FL_ERR_INVALID_ARGUMENT, ptr
+    row_ptr = np.array([0, 1, 2], np.uint32)
+    col = np.array([1, 0], np.uint32)
+    length = np.ones(2)
+    area = np.ones(2)
+    h = ctypes.c_void_p()
+    assert fl_lib.fl_graph_create(2, ptr(row_ptr), ptr(col), None, ptr(area), None, 0, None,
+                                  None, ctypes.byref(h)) == FL_ERR_INVALID_ARGUMENT
+    assert fl_lib.fl_graph_create(2, ptr(row_ptr), None, ptr(length), ptr(area), None, 0, None,
+                                  None, ctypes.byref(h)) == FL_ERR_INVALID_ARGUMENT
