@@ -560,7 +560,7 @@ extern "C" {
 // StdRng::from_seed([0; 32]) when zero_seed != 0 (fastlem's from_random_sites).
 int fl_random_sites(uint64_t n, double x0, double y0, double x1, double y1, uint64_t seed,
                     int zero_seed, double* xs, double* ys) {
-    if (!(x0 < x1) || !(y0 < y1)) return FL_ERR_INVALID_ARGUMENT;
+    if (!(x0 < x1) || !(y0 < y1) || (n && (!xs || !ys))) return FL_ERR_INVALID_ARGUMENT;
     fl::StdRng rng = zero_seed ? fl::StdRng::zero_key() : fl::StdRng::seed_from_u64(seed);
     for (uint64_t i = 0; i < n; ++i) {
         xs[i] = rng.gen_range(x0, x1);
@@ -574,6 +574,7 @@ int fl_random_sites(uint64_t n, double x0, double y0, double x1, double y1, uint
 // FL_ERR_BUILDER_VORONOI when the triangulation fails (ModelBuilderError::VoronoiError).
 int fl_relax_sites(uint32_t n, double* xs, double* ys, double x0, double y0, double x1, double y1,
                    uint32_t times) {
+    if (times && (!xs || !ys)) return FL_ERR_INVALID_ARGUMENT;
     std::vector<double> area(n), cx(n), cy(n);
     for (uint32_t r = 0; r < times; ++r) {
         fl::SweepHull d{xs, ys, n};
@@ -595,6 +596,8 @@ int fl_build_graph(uint32_t n, const double* xs, const double* ys, double x0, do
                    double x1, double y1, uint32_t* row_ptr, uint32_t* col, double* len,
                    uint64_t cap, double* area, uint32_t* hull, uint64_t* out_nnz,
                    uint32_t* out_nhull) {
+    if (!xs || !ys || !row_ptr || !col || !len || !area || !hull || !out_nnz || !out_nhull)
+        return FL_ERR_INVALID_ARGUMENT;
     fl::SweepHull d{xs, ys, n};
     if (!d.run()) return FL_ERR_BUILDER_VORONOI;
     std::vector<uint32_t> h = d.hull();
@@ -633,6 +636,7 @@ int fl_build_graph(uint32_t n, const double* xs, const double* ys, double x0, do
 // count, or -1 on failure.  `tri` holds up to `cap` triangles.
 int64_t fl_triangulate(uint32_t n, const double* xs, const double* ys, uint32_t* tri,
                        uint64_t cap) {
+    if (!xs || !ys) return -1;
     fl::SweepHull d{xs, ys, n};
     if (!d.run()) return -1;
     uint64_t ntri = d.tri.size() / 3;

@@ -95,3 +95,17 @@ def test_add_edge_sites(fl_lib):
     # sqrt(400 / 100 * 100) = 20 sites per side, 4 sides
     assert len(e.xs) == 400 + 80
     assert e.build().num() == 480
+
+
+def test_builder_entry_points_reject_null_arrays(fl_lib):
+    """The C builder calls check their arrays before touching them."""
+    from fastlem_gb300._lib import FL_ERR_INVALID_ARGUMENT
+    import ctypes
+    xs = np.array([0.0, 1.0, 0.0, 1.0])
+    ys = np.array([0.0, 0.0, 1.0, 1.0])
+    assert fl_lib.fl_random_sites(4, 0.0, 0.0, 1.0, 1.0, 0, 0, None, None) == FL_ERR_INVALID_ARGUMENT
+    assert fl_lib.fl_relax_sites(4, None, None, 0.0, 0.0, 1.0, 1.0, 1) == FL_ERR_INVALID_ARGUMENT
+    nnz, nh = ctypes.c_uint64(), ctypes.c_uint32()
+    assert fl_lib.fl_build_graph(4, ptr(xs), ptr(ys), 0.0, 0.0, 1.0, 1.0, None, None, None, 24,
+                                 None, None, ctypes.byref(nnz), ctypes.byref(nh)) == FL_ERR_INVALID_ARGUMENT
+    assert fl_lib.fl_triangulate(4, None, None, None, 0) == -1
