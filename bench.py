@@ -196,13 +196,48 @@ def make_workload(args):
 
 def run_cpu_sample(w, iters):
     """The oracle (CPU restatement of fastlem's generate) on this model, bounded to
-    `iters` iterations; returns (site-iterations per second, iterations, seconds)."""
+    `iters` iterations; returns (site-iterations per second, iterations, seconds,
+    elevations)."""
     from oracle import oracle as orc
     from tests import graphs
     p = w.params
     r = orc.generate(graphs.from_model(w.model), p.base, p.erodibility, p.uplift, p.is_outlet,
                      max_slope=p.max_slope, max_iter=iters)
-    return w.model.num() * r["iters"] / r["seconds"], r["iters"], r["seconds"]
+    return w.model.num() * r["iters"] / r["seconds"], r["iters"], r["seconds"], r["elev"]
+
+
+def gpu_matches_cpu_sample(w, iters, want_iters, want_elev):
+    """The GPU's generate() with the CPU sample's iteration bound, compared bit for bit
+    with the sample's elevations (the measured CPU work is the same solve)."""
+    from fastlem_gb300 import TerrainGenerator
+    gen = (TerrainGenerator.default().set_model(w.model).set_parameters(w.params)
+           .set_max_iteration(iters))
+    got = gen.generate().elevations()
+    same = (gen.last_iterations == want_iters and
+            np.array_equal(np.ascontiguousarray(got).view(np.uint64),
+                           np.ascontiguousarray(want_elev).view(np.uint64)))
+    return {"iterations": int(want_iters), "bit_exact": bool(same)}
+
+
+def cold_call(w, iters):
+    """What a drop-in generate() pays when it builds its model each call: a fresh
+    device graph (Hilbert order, CSR relabelling, upload) and a first generate() that
+    also computes the lake order, from pageable host arrays, host-timed."""
+    from fastlem_gb300 import TerrainGenerator
+    from fastlem_gb300.api import TerrainModel2D
+    m = w.model
+    fresh = TerrainModel2D(m.xs, m.ys, m.area, m.row_ptr, m.col, m.length, m.default_outlets)
+    t0 = time.perf_counter()
+    fresh.handle()
+    t1 = time.perf_counter()
+    gen = TerrainGenerator.default().set_model(fresh).set_parameters(w.params).set_max_iteration(iters)
+    gen.generate()
+    t2 = time.perf_counter()
+    fresh.release()
+    return {"graph_create_s": t1 - t0, "first_generate_s": t2 - t1, "total_s": t2 - t0,
+            "iterations": gen.last_iterations,
+            "what": "fl_graph_create + first fl_generate (lake order included), pageable "
+                    "host arrays, host wall clock"}
 
 
 def cpu_pool_sample(models, params, iters, per_terrain_iters, budget_s=12.0):
@@ -387,14 +422,24 @@ def bench_gpu(args, d):
                             "achieved": whole, "frac": whole / peak}}
     share = {k: round(v[1] / max(1e-9, sum(x[1] for x in stats.values())), 4)
              for k, v in stats.items() if v[0]}
+    # loop time on the device not covered by any launch group: launch latency and the
+    # host round trips of the iteration loop
+    idle = {"ms_per_step": (loop_ms - all_ms) / args.steps,
+            "frac": (loop_ms - all_ms) / loop_ms if loop_ms else 0.0,
+            "host_syncs_per_iteration": _lib.host_syncs(h) / max(1, iters)}
     cpu = None
     if not args.no_cpu_baseline and args.gpus == 1:
         from oracle import build as ob
         ob.build()
-        v, it, s = run_cpu_sample(w, args.cpu_iters)
+        v, it, s, elev = run_cpu_sample(w, args.cpu_iters)
         cpu = {"value": v / 1e6, "unit": "Msite-iters/s", "cores": 1, "kind": "port",
                "sample": f"oracle generate() with set_max_iteration({it}) on the same {n:,}-site "
-                         f"model, {s:.1f} s, 1 thread", "host_cores": os.cpu_count()}
+                         f"model, {s:.1f} s, 1 thread", "host_cores": os.cpu_count(),
+               "gpu_parity": gpu_matches_cpu_sample(w, args.cpu_iters, it, elev),
+               "parity_note": "GPU results equal the oracle bit for bit; the oracle restates "
+                              "fastlem's generate() and is not pinned against fastlem's own "
+                              "binary (no Rust toolchain, no reference goldens)"}
+        del elev
     # base, erodibility, uplift, is_outlet (+ max_slope when given), from pinned memory
     h2d = n * (8 + 8 + 8 + 1) + (n * 8 if p.max_slope is not None else 0)
     d2h = n * 8
@@ -414,10 +459,13 @@ def bench_gpu(args, d):
         "cpu_baseline": cpu,
         "gpu_launches": launches,
         "kernel_time_share": share,
+        "idle_gap": idle,
         "basin_last_iteration": basin,
         "clocks": clocks.summary(),
         "wall_ms_timed": wall_ms,
     }
+    if args.gpus == 1:
+        line["cold_call"] = cold_call(w, args.iters)
     if not args.no_extras and args.gpus == 1 and args.config == "16m":
         # the other two parts of the headline metric, on the same GPU after the 16M run
         import copy

@@ -28,7 +28,8 @@ FL_ERR_DEVICE_LIMIT = 23
 EXPORTS = [
     "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
-    "fl_graph_set_timing", "fl_graph_reset_stats", "fl_num_kernel_classes", "fl_graph_kernel_stats",
+    "fl_graph_set_timing", "fl_graph_reset_stats", "fl_graph_host_syncs", "fl_num_kernel_classes",
+    "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
     "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate", "fl_graph_device_bytes",
     "fl_model_device_bytes", "fl_host_alloc", "fl_host_free",
@@ -97,6 +98,8 @@ def lib():
     L.fl_graph_set_timing.argtypes = [vp, c_int]
     L.fl_graph_reset_stats.argtypes = [vp]
     L.fl_graph_reset_stats.restype = None
+    L.fl_graph_host_syncs.argtypes = [vp]
+    L.fl_graph_host_syncs.restype = c_u64
     L.fl_num_kernel_classes.restype = c_u32
     L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
     L.fl_graph_basin_stats.argtypes = [vp, vp, c_u32]
@@ -186,6 +189,11 @@ def kernel_stats(handle):
                                       ctypes.byref(b)))
         out[name.value.decode()] = (n.value, ms.value, b.value)
     return out
+
+
+def host_syncs(handle):
+    """Blocking host synchronisations of a model handle since its last stats reset."""
+    return int(lib().fl_graph_host_syncs(handle))
 
 
 BASIN_STATS = ["kahn_rounds", "leaves", "skeleton_sites", "chains", "longest_chain", "slow_sites",

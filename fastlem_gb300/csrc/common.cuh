@@ -18,7 +18,10 @@ enum Flag {
     kBarrier = 4,   // grid barrier arrival counter
     kBarrierGen = 5,// grid barrier generation
     kExact = 6,     // receiver scans that needed the exact f64 fallback
-    kNumFlags = 8
+    kJump0 = 8,     // rotating "a label moved" words of the pointer-jumping rounds
+    kJump1 = 9,
+    kJump2 = 10,
+    kNumFlags = 16
 };
 
 // Values stored in flags[kError].

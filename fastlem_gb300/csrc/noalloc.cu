@@ -12,11 +12,18 @@
 // 256 B).  Every GPU that loads this library holds it until the process exits.
 // Host code cannot use the array's name as a device address, so the address is taken
 // once per device with cudaGetSymbolAddress, by the first call made with that device
-// current; make that first call before any stream capture.  All calls share the
-// array and it keeps the last call's contents: the status words are cleared at the
-// start of each round, the label buffer is fully rewritten.  Two calls that overlap
-// on the same GPU (different streams or threads) race on the scratch, so callers
-// must serialise them.
+// current; make that first call before any stream capture.  The address is kept for
+// the life of the process: after a cudaDeviceReset the module is loaded again and
+// the array may move, so this entry point must not be called on a device after that
+// device was reset.  All calls share the array and it keeps the last call's
+// contents: the status words are cleared at the start of each call and round, the
+// label buffer is fully rewritten.  Two calls that overlap on the same GPU (different
+// streams or threads) race on the scratch, so callers must serialise them.
+//
+// Pointer jumping settles in ceil(log2(longest path)) rounds on a forest.  A receiver
+// cycle either keeps moving (the round limit reports it) or, for a cycle whose length
+// is a power of two, settles with every cycle site labelled as itself; the final check
+// catches that case: every label must be an outlet or a site that is its own receiver.
 
 #include <cuda_runtime.h>
 
@@ -93,12 +100,21 @@ __global__ void k_na_jump(uint32_t n, const uint32_t* __restrict__ in, uint32_t*
     if (__syncthreads_or(moved) && threadIdx.x == 0) status[0] = 1;
 }
 
-// has_lake: some site drains to a root that is not an outlet (stream_tree.rs:156-158).
-__global__ void k_na_lake(uint32_t n, const uint32_t* __restrict__ lab,
-                          const uint8_t* __restrict__ outlet, uint32_t* __restrict__ status) {
+// has_lake: some site drains to a root that is not an outlet (stream_tree.rs:156-158),
+// status[1].  A label that is neither an outlet nor its own receiver is a site on a
+// receiver cycle (pointer jumping settled on it): status[3].
+__global__ void k_na_lake(uint32_t n, const uint32_t* __restrict__ next,
+                          const uint32_t* __restrict__ lab, const uint8_t* __restrict__ outlet,
+                          uint32_t* __restrict__ status) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool lake = i < n && !outlet[lab[i]];
+    bool lake = false, cycle = false;
+    if (i < n) {
+        const uint32_t l = lab[i];
+        lake = !outlet[l];
+        cycle = lake && next[l] != l;
+    }
     if (__syncthreads_or(lake) && threadIdx.x == 0) status[1] = 1;
+    if (__syncthreads_or(cycle) && threadIdx.x == 0) status[3] = 1;
 }
 
 __global__ void k_na_copy(uint32_t n, const uint32_t* __restrict__ in, uint32_t* __restrict__ out) {
@@ -123,6 +139,10 @@ extern "C" {
 int fl_basin_labels_noalloc(uint32_t n, const uint32_t* next, const uint8_t* outlet_table,
                             uint32_t* labels, int* has_lake, void* stream) {
     fl::set_last_error("");
+    if (n == 0) {                          // nothing to label: the arrays are not read
+        if (has_lake) *has_lake = 0;
+        return FL_OK;
+    }
     if (n > kNoAllocMaxSites) {
         char buf[160];
         snprintf(buf, sizeof buf,
@@ -134,10 +154,6 @@ int fl_basin_labels_noalloc(uint32_t n, const uint32_t* next, const uint8_t* out
     if (!next || !outlet_table || !labels) {
         fl::set_last_error("fl_basin_labels_noalloc: null device array");
         return FL_ERR_INVALID_ARGUMENT;
-    }
-    if (n == 0) {
-        if (has_lake) *has_lake = 0;
-        return FL_OK;
     }
     uint32_t* scratch = nullptr;
     int rc = scratch_address(&scratch);
@@ -181,13 +197,16 @@ int fl_basin_labels_noalloc(uint32_t n, const uint32_t* next, const uint8_t* out
         k_na_copy<<<grid, fl::kThreads, 0, st>>>(n, cur, labels);
         NA_CU(cudaGetLastError());
     }
-    NA_CU(cudaMemsetAsync(status + 1, 0, sizeof(uint32_t), st));
-    k_na_lake<<<grid, fl::kThreads, 0, st>>>(n, labels, outlet_table, status);
+    k_na_lake<<<grid, fl::kThreads, 0, st>>>(n, next, labels, outlet_table, status);
     NA_CU(cudaGetLastError());
-    uint32_t lake = 0;
-    NA_CU(cudaMemcpyAsync(&lake, status + 1, sizeof lake, cudaMemcpyDeviceToHost, st));
+    uint32_t words[4] = {0, 0, 0, 0};
+    NA_CU(cudaMemcpyAsync(words, status, sizeof words, cudaMemcpyDeviceToHost, st));
     NA_CU(cudaStreamSynchronize(st));
-    if (has_lake) *has_lake = lake ? 1 : 0;
+    if (words[3]) {
+        fl::set_last_error("fl_basin_labels_noalloc: receivers contain a cycle");
+        return FL_ERR_DEVICE_LIMIT;
+    }
+    if (has_lake) *has_lake = words[1] ? 1 : 0;
     return FL_OK;
 }
 

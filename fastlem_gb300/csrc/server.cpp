@@ -103,21 +103,26 @@ void drop_idle(fl_server* s, uint32_t model, fl_graph* g) {
     v.erase(std::remove(v.begin(), v.end(), g), v.end());
 }
 
+enum Admission { kWait = 0, kAdmit, kNever };
+
 // With the lock held: can the head request start now?  Takes an idle instance
 // (*inst) or reserves budget for a new one (*reserve), evicting idle instances of
-// other models as needed (collected in *evict, destroyed outside the lock).
-bool admit(fl_server* s, Request* r, fl_graph** inst, uint64_t* reserve,
-           std::vector<fl_graph*>* evict) {
+// other models as needed (collected in *evict, destroyed outside the lock).  kNever:
+// no instance of the model is idle and a new one is larger than the whole budget (the
+// measured size of an earlier instance can exceed the bound checked at submission).
+Admission admit(fl_server* s, Request* r, fl_graph** inst, uint64_t* reserve,
+                std::vector<fl_graph*>* evict) {
     Model& m = *s->models[r->model];
     if (!m.idle.empty()) {
         *inst = m.idle.back();
         drop_idle(s, r->model, *inst);
-        return true;
+        return kAdmit;
     }
     const uint64_t need = footprint(m);
+    if (need > s->budget) return kNever;
     uint64_t freeable = 0;
     for (auto& e : s->lru) freeable += s->models[e.first]->bytes;
-    if (s->used + need > s->budget + freeable) return false;
+    if (s->used + need > s->budget + freeable) return kWait;
     while (s->used + need > s->budget && !s->lru.empty()) {
         auto e = s->lru.front();
         s->lru.pop_front();
@@ -130,7 +135,7 @@ bool admit(fl_server* s, Request* r, fl_graph** inst, uint64_t* reserve,
     s->used += need;
     *reserve = need;
     *inst = nullptr;
-    return true;
+    return kAdmit;
 }
 
 void worker(fl_server* s) {
@@ -141,14 +146,27 @@ void worker(fl_server* s) {
         fl_graph* inst = nullptr;
         uint64_t reserve = 0;
         std::vector<fl_graph*> evict;
+        bool never = false;
         s->cv_work.wait(lk, [&] {
             if (s->stop) return true;
             if (s->queue.empty()) return false;
-            return admit(s, s->queue.front(), &inst, &reserve, &evict);
+            const Admission a = admit(s, s->queue.front(), &inst, &reserve, &evict);
+            never = a == kNever;
+            return a != kWait;
         });
         if (s->stop) return;
         r = s->queue.front();
         s->queue.pop_front();
+        if (never) {                          // fails alone; the requests behind it go on
+            r->status = FL_ERR_OUT_OF_MEMORY;
+            r->error = "fl_server: the model's instance is larger than the HBM budget";
+            r->started = r->finished = Clock::now();
+            r->done = true;
+            s->completed++;
+            s->cv_done.notify_all();
+            s->cv_work.notify_all();
+            continue;
+        }
         Model& m = *s->models[r->model];
         m.busy++;
         s->active++;

@@ -169,22 +169,52 @@ __global__ void k_copy_u32(uint32_t n, const uint32_t* __restrict__ a, uint32_t*
     if (i < n) b[i] = a[i];
 }
 
-// One pointer-jumping round: lab_out[i] = lab_in[lab_in[i]].  Roots (next[r] == r)
-// are fixed points, so after ceil(log2(depth)) rounds lab[i] is the basin root
-// (stream_tree.rs:139-173, "subroot").
-__global__ void k_jump(uint32_t n, const uint32_t* __restrict__ lab_in,
-                       uint32_t* __restrict__ lab_out, int* __restrict__ flags) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t l = lab_in[i];
-    uint32_t ll = lab_in[l];
-    lab_out[i] = ll;
-    if (ll != l) flags[fl::kJumped] = 1;
+// Basin labels of the receivers by pointer jumping, every round in one cooperative
+// launch: lab = next, then lab[i] = lab[lab[i]] until no label moves.  Roots
+// (next[r] == r) are fixed points, so after ceil(log2(depth)) rounds every site holds
+// its basin root (stream_tree.rs:139-173, "subroot"); the rounds synchronise on the
+// grid barrier and a rotating "moved" word, and the result ends in lab.  With a gate,
+// nothing runs unless *gate is set (the receivers found a lake), so the launch can be
+// enqueued before the host knows.
+__global__ void k_labels(uint32_t n, const uint32_t* __restrict__ next, uint32_t* lab,
+                         uint32_t* lab2, const int* gate, int* flags) {
+    if (gate && *gate == 0) return;                      // the same verdict for every block
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = gtid; i < n; i += stride) lab[i] = next[i];
+    if (!grid_barrier(flags)) return;
+    uint32_t* cur = lab;
+    uint32_t* out = lab2;
+    for (uint32_t round = 0; round < 64; ++round) {
+        int* moved_word = &flags[kJump0 + round % 3];
+        if (gtid == 0) flags[kJump0 + (round + 1) % 3] = 0;
+        bool moved = false;
+        for (uint32_t i = gtid; i < n; i += stride) {
+            const uint32_t l = __ldcg(&cur[i]);
+            const uint32_t ll = __ldcg(&cur[l]);
+            out[i] = ll;
+            moved |= ll != l;
+        }
+        if (__syncthreads_or(moved) && threadIdx.x == 0) atomicOr(moved_word, 1);
+        if (!grid_barrier(flags)) return;
+        uint32_t* t = cur;
+        cur = out;
+        out = t;
+        if (ld_acquire(moved_word) == 0) {
+            if (cur != lab)
+                for (uint32_t i = gtid; i < n; i += stride) lab[i] = __ldcg(&cur[i]);
+            return;
+        }
+    }
+    if (gtid == 0) set_error(flags, kErrForest);          // a receiver cycle
 }
 
-__global__ void k_fill_u64(uint32_t n, uint64_t* __restrict__ a, uint64_t v) {
+// best[L] = no key, for every site (gated like k_labels).
+__global__ void k_clear_keys(uint32_t n, unsigned long long* __restrict__ best,
+                             const int* gate) {
+    if (gate && *gate == 0) return;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) a[i] = v;
+    if (i < n) best[i] = kNoKey;
 }
 
 // For every site v the lake heap processes (rank[v] != none) and every neighbour j
@@ -194,7 +224,8 @@ __global__ void k_fill_u64(uint32_t n, uint64_t* __restrict__ a, uint64_t v) {
 __global__ void k_lake_keys(uint32_t n, const uint32_t* __restrict__ row,
                             const uint32_t* __restrict__ col, const uint32_t* __restrict__ rank,
                             const uint32_t* __restrict__ lab, const uint8_t* __restrict__ outlet,
-                            unsigned long long* __restrict__ best) {
+                            unsigned long long* __restrict__ best, const int* gate) {
+    if (gate && *gate == 0) return;
     uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
     uint32_t r = rank[v];
@@ -216,7 +247,8 @@ __global__ void k_lake_flip(uint32_t n, const uint32_t* __restrict__ row,
                             const uint32_t* __restrict__ col, const double* __restrict__ len,
                             const unsigned long long* __restrict__ best,
                             const uint32_t* __restrict__ site_of_rank, uint32_t* next,
-                            double* rlen, int* flags) {
+                            double* rlen, int* flags, const int* gate) {
+    if (gate && *gate == 0) return;
     uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= n) return;
     unsigned long long key = best[L];
@@ -261,6 +293,28 @@ __global__ void k_fill_f64(uint32_t n, double* __restrict__ a, const double* __r
     if (i < n) a[i] = src ? src[i] : 0.0;
 }
 
+// Packed terrains: a terrain whose elevations did not change in iteration `iter`
+// (1-based) would have stopped there alone; its first such iteration is recorded, and
+// the per-terrain "changed" words are cleared for the next iteration.
+__global__ void k_terrain_iters(uint32_t terrains, int* __restrict__ tchg,
+                                uint32_t* __restrict__ titer, uint32_t iter) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= terrains) return;
+    if (!tchg[t] && titer[t] == 0) titer[t] = iter;
+    tchg[t] = 0;
+}
+
+// Blocks of `block` threads at which `kernel` is co-resident on the current device,
+// at most cap_per_sm per SM.
+unsigned coop_blocks(const void* kernel, unsigned block, unsigned cap_per_sm) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, (int)block, 0);
+    if (per < 1) per = 1;
+    return (unsigned)(sms * std::min<unsigned>((unsigned)per, cap_per_sm));
+}
+
 }  // namespace
 
 namespace fl {
@@ -302,7 +356,11 @@ struct fl_graph {
     uint32_t* d_noise_idx = nullptr;   // device site -> its sample (index within its terrain)
     uint32_t* d_tid = nullptr;
     int* d_tchg = nullptr;
-    std::vector<int> h_tchg;
+    uint32_t* d_titer = nullptr;   // per terrain: first iteration without a change (0: none yet)
+    // page-locked copy of the status words and basin-pass bookkeeping, read once per
+    // iteration
+    int* h_status = nullptr;
+    uint64_t host_syncs = 0;       // blocking stream synchronisations inside generate()
     // model (device)
     uint32_t *d_row = nullptr, *d_col = nullptr;
     double *d_len = nullptr, *d_area = nullptr;
@@ -381,9 +439,10 @@ void free_graph(fl_graph* g) {
                     g->d_tokval, g->d_needl, g->d_push, g->d_rtime, g->d_kslot, g->d_cpar,
                     g->d_cqp, g->d_trec, g->d_noise_idx, g->d_tid, g->d_tchg, g->d_cdep,
                     g->d_cpar1, g->d_cdep1, g->d_chist, g->d_corder, g->d_tokslot, g->d_pend,
-                    g->d_corder_up, g->d_wa, g->d_wl, g->d_ilen};
+                    g->d_corder_up, g->d_wa, g->d_wl, g->d_ilen, g->d_titer};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (g->h_status) cudaFreeHost(g->h_status);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
     for (auto& p : g->ev_pending) {
         cudaEventDestroy(p.second.first);
@@ -528,20 +587,32 @@ int alloc_workspace(fl_graph* g) {
     FL_CU(cudaMemset(g->d_td_done, 0, n * 4ull));
     FL_CU(cudaMemset(g->d_push, 0, n * 8ull));
     FL_CU(cudaMemset(g->d_flags, 0, kNumFlags * 4ull));
+    FL_CU(cudaHostAlloc((void**)&g->h_status, (kNumFlags + kMetaCount) * sizeof(int),
+                        cudaHostAllocPortable));
     return FL_OK;
 }
 
-int read_flags(fl_graph* g, int* h) {
-    FL_CU(cudaMemcpyAsync(h, g->d_flags, kNumFlags * sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+// The status words (and, with meta, the basin pass's bookkeeping words) back to the
+// host: one blocking synchronisation of the model's stream.
+int sync_status(fl_graph* g, int* h, bool meta = false) {
+    FL_CU(cudaMemcpyAsync(g->h_status, g->d_flags, kNumFlags * sizeof(int), cudaMemcpyDeviceToHost,
+                          g->stream));
+    if (meta)
+        FL_CU(cudaMemcpyAsync(g->h_status + kNumFlags, g->d_meta, kMetaCount * sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, g->stream));
     FL_CU(cudaStreamSynchronize(g->stream));
+    g->host_syncs++;
+    std::memcpy(h, g->h_status, kNumFlags * sizeof(int));
+    if (meta) std::memcpy(g->last_meta, g->h_status + kNumFlags, sizeof g->last_meta);
     return FL_OK;
 }
 
-// Clears the per-iteration status words (not the barrier words, which the grid
-// barrier leaves consistent).
+// Clears the per-iteration status words: has_lake, changed, error, the exact-scan count
+// and the pointer-jumping words (not the barrier words, which the grid barrier leaves
+// consistent).
 int clear_flags(fl_graph* g) {
     FL_CU(cudaMemsetAsync(g->d_flags, 0, 4 * sizeof(int), g->stream));
-    FL_CU(cudaMemsetAsync(g->d_flags + kExact, 0, sizeof(int), g->stream));
+    FL_CU(cudaMemsetAsync(g->d_flags + kExact, 0, (kJump2 + 1 - kExact) * sizeof(int), g->stream));
     return FL_OK;
 }
 
@@ -675,61 +746,44 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
     return FL_OK;
 }
 
-// Receivers for the current elevations; *has_lake from the device flag.
-int run_receivers(fl_graph* g, int* has_lake) {
-    FL_TRY(clear_flags(g));
+// Receivers for the current elevations; the kernel raises flags[kHasLake].
+int enqueue_receivers(fl_graph* g) {
     FL_LAUNCH(g, kcReceivers, 25.0 * g->n + 20.0 * g->nnz,
               fl::launch_receivers(g->stream, g->n, g->d_row, g->d_col, g->d_len, g->d_ilen,
                                    g->d_elev, g->d_outlet, g->d_next, g->d_rlen, g->d_flags));
     FL_CU(cudaGetLastError());
-    int h[kNumFlags];
-    FL_TRY(read_flags(g, h));
-    *has_lake = h[kHasLake];
     return FL_OK;
 }
 
-// Basin labels of d_next into d_lab (pointer jumping).
-int run_labels(fl_graph* g) {
+// Basin labels of d_next into d_lab (pointer jumping, one cooperative launch); with a
+// gate, only if *gate is set when the kernel runs.
+int enqueue_labels(fl_graph* g, const int* gate) {
     uint32_t n = g->n;
+    static const unsigned grid = coop_blocks((const void*)k_labels, 1024, 2);
+    const int* gt = gate;
+    void* argv[] = {(void*)&n, (void*)&g->d_next, (void*)&g->d_lab, (void*)&g->d_lab2,
+                    (void*)&gt, (void*)&g->d_flags};
     FL_LAUNCH(g, kcLakes, 8.0 * n,
-              k_copy_u32<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_next, g->d_lab));
+              cudaLaunchCooperativeKernel((const void*)k_labels, dim3(grid), dim3(1024), argv, 0,
+                                          g->stream));
     FL_CU(cudaGetLastError());
-    for (int round = 0;; ++round) {
-        if (round > 64) {
-            g_err = "basin labelling did not converge";
-            return FL_ERR_DEVICE_LIMIT;
-        }
-        FL_TRY(clear_flags(g));
-        FL_LAUNCH(g, kcLakes, 12.0 * n,
-                  k_jump<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_lab, g->d_lab2,
-                                                                   g->d_flags));
-        FL_CU(cudaGetLastError());
-        std::swap(g->d_lab, g->d_lab2);
-        int h[kNumFlags];
-        FL_TRY(read_flags(g, h));
-        if (!h[kJumped]) break;
-    }
     return FL_OK;
 }
 
-// Lake re-routing on d_next (labels must be current).
-int run_lakes(fl_graph* g) {
+// Lake re-routing on d_next (labels must be current), gated like enqueue_labels.
+int enqueue_lakes(fl_graph* g, const int* gate) {
     uint32_t n = g->n;
-    FL_TRY(clear_flags(g));
     FL_LAUNCH(g, kcLakes, 8.0 * n,
-              k_fill_u64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, (uint64_t*)g->d_best,
-                                                                      kNoKey));
+              k_clear_keys<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_best, gate));
     FL_LAUNCH(g, kcLakes, 12.0 * n + 8.0 * g->nnz,
               k_lake_keys<<<blocks_for(n), kThreads, 0, g->stream>>>(
-                  n, g->d_row, g->d_col, g->d_rank, g->d_lab, g->d_outlet, g->d_best));
+                  n, g->d_row, g->d_col, g->d_rank, g->d_lab, g->d_outlet, g->d_best, gate));
     FL_LAUNCH(g, kcLakes, 8.0 * n,
               k_lake_flip<<<blocks_for(n), kThreads, 0, g->stream>>>(
                   n, g->d_row, g->d_col, g->d_len, g->d_best, g->d_sor, g->d_next, g->d_rlen,
-                  g->d_flags));
+                  g->d_flags, gate));
     FL_CU(cudaGetLastError());
-    int h[kNumFlags];
-    FL_TRY(read_flags(g, h));
-    return device_error(h);
+    return FL_OK;
 }
 
 // Drainage areas, response times, elevations on final receivers; *changed.
@@ -753,9 +807,10 @@ void account_skeleton(fl_graph* g) {
     g->k_bytes[kcSkelRank] += 24.0 * ns * rounds;
 }
 
-// all_records: every site's top-down record is read afterwards (response times)
-int run_basin_pass(fl_graph* g, int* changed, bool all_records = false) {
-    FL_TRY(clear_flags(g));
+// Enqueues the pass; flags[kChanged] / flags[kError] and the bookkeeping words in meta
+// hold its outcome once it has run (finish_basin_pass).  all_records: every site's
+// top-down record is read afterwards (response times).
+int enqueue_basin_pass(fl_graph* g, bool all_records = false) {
     g->stamp = g->stamp == 0x7ffffff0 ? 1 : g->stamp + 1;
     if (g->stamp == 1) {   // stamps wrapped (or first pass): clear hand-off words
         FL_CU(cudaMemsetAsync(g->d_bu_done, 0, g->n * 4ull, g->stream));
@@ -846,14 +901,15 @@ int run_basin_pass(fl_graph* g, int* changed, bool all_records = false) {
         return e == cudaErrorMemoryAllocation ? FL_ERR_OUT_OF_MEMORY : FL_ERR_CUDA;
     }
     FL_CU(cudaGetLastError());
-    FL_CU(cudaMemcpyAsync(g->last_meta, g->d_meta, sizeof g->last_meta, cudaMemcpyDeviceToHost,
-                          g->stream));
-    int h[kNumFlags];
-    FL_TRY(read_flags(g, h));
+    return FL_OK;
+}
+
+// After sync_status(.., meta = true) following a pass: its device error, if any, and
+// the bookkeeping that needs the skeleton's size.
+int finish_basin_pass(fl_graph* g, const int* h) {
     FL_TRY(device_error(h));
     g->w_valid = true;
     account_skeleton(g);
-    *changed = h[kChanged];
     return FL_OK;
 }
 
@@ -924,31 +980,53 @@ int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const doub
     g->passes = 0;
     // a terrain alone stops at its first iteration without a change; packed with others
     // it keeps iterating at a fixed point, so its count is that first unchanged iteration
-    std::vector<uint32_t> t_iters(g->terrains, 0);
+    if (g->d_titer) {
+        FL_CU(cudaMemsetAsync(g->d_tchg, 0, g->terrains * sizeof(int), g->stream));
+        FL_CU(cudaMemsetAsync(g->d_titer, 0, g->terrains * sizeof(uint32_t), g->stream));
+    }
+    // One blocking synchronisation per iteration, after the basin pass: whether an
+    // elevation changed (the loop's exit, generator.rs:207-209) and any device error.
+    // The lake stages are enqueued behind the receivers and skip themselves when the
+    // receivers found no lake; only while the lake order for this outlet list is not on
+    // the device yet does the host wait for the receivers' lake flag to compute it.
     for (uint64_t it = 0; it < limit; ++it) {
         ++iters;
-        int has_lake = 0, changed = 0;
-        FL_TRY(run_receivers(g, &has_lake));
-        if (has_lake) {
-            FL_TRY(set_outlets(g, outlets, true));
-            FL_TRY(run_labels(g));
-            FL_TRY(run_lakes(g));
+        int h[kNumFlags];
+        FL_TRY(clear_flags(g));
+        FL_TRY(enqueue_receivers(g));
+        bool lakes = true;
+        const int* gate = g->d_flags + kHasLake;
+        if (!g->rank_uploaded) {
+            FL_TRY(sync_status(g, h));
+            lakes = h[kHasLake] != 0;
+            gate = nullptr;
+            if (lakes) FL_TRY(set_outlets(g, outlets, true));
         }
-        if (g->d_tchg)
-            FL_CU(cudaMemsetAsync(g->d_tchg, 0, g->terrains * sizeof(int), g->stream));
-        FL_TRY(run_basin_pass(g, &changed));
-        if (g->d_tchg) {
-            FL_CU(cudaMemcpyAsync(g->h_tchg.data(), g->d_tchg, g->terrains * sizeof(int),
+        if (lakes) {
+            FL_TRY(enqueue_labels(g, gate));
+            FL_TRY(enqueue_lakes(g, gate));
+        }
+        FL_TRY(enqueue_basin_pass(g));
+        if (g->d_titer) {
+            k_terrain_iters<<<blocks_for(g->terrains), kThreads, 0, g->stream>>>(
+                g->terrains, g->d_tchg, g->d_titer, iters);
+            FL_CU(cudaGetLastError());
+        }
+        FL_TRY(sync_status(g, h, true));
+        FL_TRY(finish_basin_pass(g, h));
+        if (!h[kChanged]) break;
+    }
+    if (terrain_iters) {
+        if (g->d_titer) {
+            FL_CU(cudaMemcpyAsync(terrain_iters, g->d_titer, g->terrains * sizeof(uint32_t),
                                   cudaMemcpyDeviceToHost, g->stream));
             FL_CU(cudaStreamSynchronize(g->stream));
             for (uint32_t t = 0; t < g->terrains; ++t)
-                if (!t_iters[t] && !g->h_tchg[t]) t_iters[t] = iters;
+                if (!terrain_iters[t]) terrain_iters[t] = iters;
+        } else {
+            terrain_iters[0] = iters;
         }
-        if (!changed) break;
     }
-    if (terrain_iters)
-        for (uint32_t t = 0; t < g->terrains; ++t)
-            terrain_iters[t] = t_iters[t] ? t_iters[t] : iters;
     FL_CU(cudaEventRecord(g->ev1, g->stream));
     FL_TRY(download_permuted(g, g->d_elev, out_elev));
     FL_CU(cudaStreamSynchronize(g->stream));
@@ -1104,9 +1182,8 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
                 nidx[j] = g->perm[j] - so[t];
                 tid[j] = t;
             }
-        g->h_tchg.assign(k_terr, 0);
         if ((rc = dalloc(&g->d_noise_idx, n)) || (rc = dalloc(&g->d_tid, n)) ||
-            (rc = dalloc(&g->d_tchg, k_terr)))
+            (rc = dalloc(&g->d_tchg, k_terr)) || (rc = dalloc(&g->d_titer, k_terr)))
             return fail(rc);
         if (cudaMemcpy(g->d_noise_idx, nidx.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(g->d_tid, tid.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -1212,8 +1289,10 @@ int fl_probe_receivers(fl_graph* g, const double* elev, const uint8_t* outlet_ta
     FL_TRY(upload_permuted(g, elev, g->d_elev));
     FL_CU(cudaMemcpyAsync(g->d_outlet, table.data(), n, cudaMemcpyHostToDevice, g->stream));
     FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
-    int hl = 0;
-    FL_TRY(run_receivers(g, &hl));
+    FL_TRY(enqueue_receivers(g));
+    int h[kNumFlags];
+    FL_TRY(sync_status(g, h));
+    const int hl = h[kHasLake];
     std::vector<uint32_t> nx(n);
     FL_CU(cudaMemcpyAsync(nx.data(), g->d_next, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
     FL_CU(cudaStreamSynchronize(g->stream));
@@ -1234,12 +1313,14 @@ int fl_probe_lakes(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     FL_CU(cudaMemcpyAsync(g->d_next, nx.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
     std::vector<double> ones(n, 1.0);
     FL_CU(cudaMemcpyAsync(g->d_rlen, ones.data(), n * 8ull, cudaMemcpyHostToDevice, g->stream));
-    FL_TRY(run_labels(g));
+    FL_TRY(enqueue_labels(g, nullptr));
     std::vector<uint32_t> lab(n);
     FL_CU(cudaMemcpyAsync(lab.data(), g->d_lab, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
-    FL_TRY(run_lakes(g));
+    FL_TRY(enqueue_lakes(g, nullptr));
     FL_CU(cudaMemcpyAsync(nx.data(), g->d_next, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
-    FL_CU(cudaStreamSynchronize(g->stream));
+    int h[kNumFlags];
+    FL_TRY(sync_status(g, h));
+    FL_TRY(device_error(h));
     for (uint32_t i = 0; i < n; ++i) {
         next_out[i] = g->perm[nx[g->inv[i]]];
         if (label_out) label_out[i] = g->perm[lab[g->inv[i]]];
@@ -1272,8 +1353,11 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     k_fill_f64<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_A, g->d_area);
     FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * sizeof(int), g->stream));
     FL_CU(cudaStreamSynchronize(g->stream));
-    int ch = 0;
-    FL_TRY(run_basin_pass(g, &ch, true));
+    FL_TRY(enqueue_basin_pass(g, true));
+    int h[kNumFlags];
+    FL_TRY(sync_status(g, h, true));
+    FL_TRY(finish_basin_pass(g, h));
+    const int ch = h[kChanged];
     FL_TRY(download_permuted(g, g->d_elev, elev));
     FL_CU(cudaStreamSynchronize(g->stream));
     if (drainage_out) {
@@ -1328,8 +1412,11 @@ int fl_graph_set_timing(fl_graph* g, int enable) {
     return FL_OK;
 }
 
+uint64_t fl_graph_host_syncs(const fl_graph* g) { return g ? g->host_syncs : 0; }
+
 void fl_graph_reset_stats(fl_graph* g) {
     if (!g) return;
+    g->host_syncs = 0;
     for (int c = 0; c < kcCount; ++c) {
         g->k_launches[c] = 0;
         g->k_ms[c] = 0;

@@ -196,6 +196,9 @@ int fl_select_device(int device);
  * device time accumulated.  Classes are numbered 0 .. fl_num_kernel_classes()-1. */
 int fl_graph_set_timing(fl_graph* g, int enable);
 void fl_graph_reset_stats(fl_graph* g);
+/* Blocking host synchronisations the model's calls made since the last reset: one per
+ * iteration of generate(), one more in an iteration that computes the lake order. */
+uint64_t fl_graph_host_syncs(const fl_graph* g);
 uint32_t fl_num_kernel_classes(void);
 int fl_graph_kernel_stats(const fl_graph* g, uint32_t cls, const char** name, uint64_t* launches,
                           double* device_ms, double* bytes);
@@ -263,9 +266,13 @@ int fl_probe_rng_f64(uint64_t seed, uint64_t first, uint64_t count, double* out)
  *   stream:             cudaStream_t (NULL = default stream)
  * Allocates nothing: the only scratch is a fixed 16 MiB device array inside the
  * library, held by every GPU that loads it, so n must not exceed 4,194,304
- * (FL_ERR_INVALID_ARGUMENT otherwise).  The first call on a device looks up that
- * array's address; make it before any stream capture.  Calls share the scratch, so
- * calls that overlap on one GPU race: serialise them. */
+ * (FL_ERR_INVALID_ARGUMENT otherwise).  n == 0 returns FL_OK with has_lake 0 and
+ * reads no array; otherwise the arrays must be non-null.  A receiver outside [0, n)
+ * gives FL_ERR_INVALID_ARGUMENT, a receiver cycle (through no outlet)
+ * FL_ERR_DEVICE_LIMIT.  The first call on a device looks up that array's address and
+ * keeps it for the life of the process; make it before any stream capture, and do
+ * not call this after a cudaDeviceReset of that device (the array may move).  Calls
+ * share the scratch, so calls that overlap on one GPU race: serialise them. */
 int fl_basin_labels_noalloc(uint32_t n, const uint32_t* next, const uint8_t* outlet_table,
                             uint32_t* labels, int* has_lake, void* stream);
 
