@@ -28,7 +28,8 @@ FL_ERR_DEVICE_LIMIT = 23
 EXPORTS = [
     "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
-    "fl_graph_set_timing", "fl_graph_reset_stats", "fl_graph_host_syncs", "fl_num_kernel_classes",
+    "fl_graph_set_timing", "fl_graph_reset_stats", "fl_graph_host_syncs", "fl_set_tuning",
+    "fl_get_tuning", "fl_num_kernel_classes",
     "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
     "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate", "fl_graph_device_bytes",
@@ -100,6 +101,9 @@ def lib():
     L.fl_graph_reset_stats.restype = None
     L.fl_graph_host_syncs.argtypes = [vp]
     L.fl_graph_host_syncs.restype = c_u64
+    L.fl_set_tuning.argtypes = [ctypes.c_char_p, ctypes.c_int64]
+    L.fl_get_tuning.argtypes = [ctypes.c_char_p]
+    L.fl_get_tuning.restype = ctypes.c_int64
     L.fl_num_kernel_classes.restype = c_u32
     L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
     L.fl_graph_basin_stats.argtypes = [vp, vp, c_u32]
@@ -189,6 +193,25 @@ def kernel_stats(handle):
                                       ctypes.byref(b)))
         out[name.value.decode()] = (n.value, ms.value, b.value)
     return out
+
+
+TUNING = ("low_ilp", "walk_per_sm", "kahn_min_width")
+
+
+def set_tuning(**kw):
+    """Sets launch-shape / switch-point knobs (see fl_set_tuning); returns the previous
+    values of the ones set."""
+    L = lib()
+    old = {}
+    for k, v in kw.items():
+        old[k] = int(L.fl_get_tuning(k.encode()))
+        check(L.fl_set_tuning(k.encode(), int(v)))
+    return old
+
+
+def get_tuning():
+    L = lib()
+    return {k: int(L.fl_get_tuning(k.encode())) for k in TUNING}
 
 
 def host_syncs(handle):

@@ -1363,13 +1363,20 @@ __global__ void k_s_finish(TopDown td, const uint32_t* __restrict__ layout,
 // Top-down over the Kahn rounds, highest round first, a grid barrier between rounds.
 // After the barrier a site only needs its receiver's record: each thread loads its
 // first site of the next round (id at the start of the round, receiver and own inputs
-// before the barrier), so a narrow round costs about one barrier and one load.
+// before the barrier), so a narrow round costs about one barrier and one load.  In a
+// wide round a thread has further sites; it takes them K at a time, issuing all K ids,
+// then all K sites' inputs, then all K receivers' records before settling any, so K
+// dependent load chains are in flight per thread instead of one (the sites of a round
+// are independent: every receiver belongs to a higher round).
 // Round 0 is the leaves, which are nobody's receiver: their records are written only
 // when all_records asks for every site's record.
-template <bool kSlope>
-__global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
-                               const uint32_t* __restrict__ roff, uint64_t* __restrict__ rtime,
-                               const uint32_t* meta, bool all_records) {
+constexpr int low_block(int K) { return K == 1 ? 1024 : K == 2 ? 512 : 256; }
+
+template <bool kSlope, int K>
+__global__ void __launch_bounds__(low_block(K))
+k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
+               const uint32_t* __restrict__ roff, uint64_t* __restrict__ rtime,
+               const uint32_t* meta, bool all_records) {
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
     if (ld_acquire(&td.flags[kError])) return;
@@ -1379,9 +1386,8 @@ __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
     struct Site {
         uint32_t v, p;
         double w, u, tn, dist, old_e;
-        bool outlet;
     };
-    // the slope inputs only with slope limits; the outlet flag only matters for a root
+    // the slope inputs only with slope limits
     auto inputs = [&](uint32_t v, Site& f) {
         f.v = v;
         f.p = td.next[v];
@@ -1390,30 +1396,47 @@ __global__ void k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
         f.tn = kSlope ? td.tanms[v] : __longlong_as_double(0x7ff8000000000000ll);
         f.dist = kSlope ? td.rlen[v] : 1.0;
         f.old_e = __ldcg(&td.elev[v]);
-        f.outlet = false;
+    };
+    // the outlet flag only matters for a root
+    auto settle_site = [&](const Site& f, const TRec& rp, bool write_rec) {
+        const bool root = f.p == f.v;
+        const bool is_outlet = root && td.outlet[f.v] != 0;
+        double en;
+        settle_own(td, f.v, root, rp, f.w, f.u, f.tn, f.dist, f.old_e, is_outlet, &en, &changed,
+                   write_rec);
     };
     Site cur{};
-    bool have = false;
-    if (rs > 0 && roff[rs - 1] + gtid < roff[rs]) {
-        inputs(order[roff[rs - 1] + gtid], cur);
-        have = true;
-    }
+    if (rs > 0 && roff[rs - 1] + gtid < roff[rs]) inputs(order[roff[rs - 1] + gtid], cur);
     for (uint32_t r = rs; r-- > 0;) {
         const uint32_t b = roff[r], e = roff[r + 1];
+        const bool write_rec = r > 0 || all_records;
         const uint32_t nidx = (r > 0 && roff[r - 1] + gtid < b) ? roff[r - 1] + gtid : kNone;
         const uint32_t nv = nidx != kNone ? order[nidx] : kNone;   // next round, in flight
-        for (uint32_t i = b + gtid; i < e; i += stride) {
-            Site f;
-            if (have && i == b + gtid) f = cur;
-            else inputs(order[i], f);
-            const TRec rp = f.p != f.v ? load_rec(&td.rec[f.p]) : TRec{};
-            if (f.p == f.v) f.outlet = td.outlet[f.v] != 0;
-            double en;
-            settle_own(td, f.v, f.p == f.v, rp, f.w, f.u, f.tn, f.dist, f.old_e, f.outlet, &en,
-                       &changed, r > 0 || all_records);
+        uint32_t i = b + gtid;
+        if (i < e) {                                   // the prefetched first site
+            const TRec rp = cur.p != cur.v ? load_rec(&td.rec[cur.p]) : TRec{};
+            settle_site(cur, rp, write_rec);
         }
-        have = nv != kNone;
-        if (have) inputs(nv, cur);
+        for (i += stride; i < e; i += K * stride) {
+            uint32_t vid[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const uint32_t ii = i + (uint32_t)k * stride;
+                vid[k] = ii < e ? order[ii] : kNone;
+            }
+            Site f[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (vid[k] != kNone) inputs(vid[k], f[k]);
+            TRec rp[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                rp[k] = (vid[k] != kNone && f[k].p != f[k].v) ? load_rec(&td.rec[f[k].p]) : TRec{};
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (vid[k] != kNone) settle_site(f[k], rp[k], write_rec);
+        }
+        if (nv != kNone) inputs(nv, cur);
         if (!grid_barrier(td.flags)) return;
         if (gtid == 0) rtime[rs - r] = global_ns();
     }
@@ -1424,6 +1447,13 @@ template <class K, class... Args>
 cudaError_t coop_launch(K kernel, unsigned grid, unsigned block, cudaStream_t st, Args... args) {
     void* argv[] = {(void*)&args...};
     return cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(block), argv, 0, st);
+}
+
+template <class... Args>
+cudaError_t coop_launch_ptr(const void* kernel, unsigned grid, unsigned block, cudaStream_t st,
+                            Args... args) {
+    void* argv[] = {(void*)&args...};
+    return cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(block), argv, 0, st);
 }
 
 // Blocks of `block` threads at which `kernel` is co-resident on the current device.
@@ -1479,13 +1509,25 @@ uint32_t walk_capacity() {
     return (uint32_t)(sms * per * kWalkWarps);
 }
 
+uint32_t walk_grid() {
+    static uint32_t cached = 0;            // the GPUs of a process match
+    if (!cached) cached = std::max<uint32_t>(1, walk_capacity() / kWalkWarps);
+    uint32_t g = cached;
+    const uint32_t per_sm = tuning().walk_per_sm;
+    if (per_sm) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        g = std::min<uint32_t>(g, (uint32_t)std::max(1, sms) * per_sm);
+    }
+    return g;
+}
+
 cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz) {
     const uint32_t n = a.n;
     const unsigned nb = (n + kThreads - 1) / kThreads;
     const unsigned g_kahn = coop_grid((const void*)k_kahn, kThreads, 8);
     const unsigned g_rank = coop_grid((const void*)k_s_rank, kRoundBlock, 2);
-    const unsigned g_low = coop_grid((const void*)k_low_top_down<false>, kRoundBlock, 2);
-    const unsigned g_low_s = coop_grid((const void*)k_low_top_down<true>, kRoundBlock, 2);
     // ordered compactions: one block range each, two blocks per SM
     const unsigned g_compact = coop_grid((const void*)k_collect_leaves, kRoundBlock, 2);
     // persistent chain walkers: every warp resident (they wait on one another)
@@ -1604,14 +1646,20 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     // top-down rounds: order 4, next 4, w 8, u 8, tan 8, rlen 8, elev 8+8, t 8, bas 4,
     // parent t/elev/bas 20, outlet t/elev 16 per site
     hk.begin(hk.ctx);
-    if (a.slope)
-        e = coop_launch(k_low_top_down<true>, g_low_s, kRoundBlock, st, td,
-                        (const uint32_t*)a.order, (const uint32_t*)a.roff,
-                        a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta, a.all_records);
-    else
-        e = coop_launch(k_low_top_down<false>, g_low, kRoundBlock, st, td,
-                        (const uint32_t*)a.order, (const uint32_t*)a.roff,
-                        a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta, a.all_records);
+    {
+        const int K = tuning().low_ilp;
+        const void* kern =
+            a.slope ? (K == 4 ? (const void*)k_low_top_down<true, 4>
+                              : K == 2 ? (const void*)k_low_top_down<true, 2>
+                                       : (const void*)k_low_top_down<true, 1>)
+                    : (K == 4 ? (const void*)k_low_top_down<false, 4>
+                              : K == 2 ? (const void*)k_low_top_down<false, 2>
+                                       : (const void*)k_low_top_down<false, 1>);
+        const unsigned blk = (unsigned)low_block(K);
+        e = coop_launch_ptr(kern, coop_grid(kern, blk, 2048 / blk), blk, st, td,
+                            (const uint32_t*)a.order, (const uint32_t*)a.roff,
+                            a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta, a.all_records);
+    }
     hk.end(hk.ctx, kcLowDown, 112.0 * n);
     return e;
 }

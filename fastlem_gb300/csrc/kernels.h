@@ -24,9 +24,23 @@ enum KClass {
 // Skeleton chains are walked one warp each, this many warps per block.
 constexpr int kWalkWarps = 4;
 
+// Tunable launch shapes and switch points, process-wide.  Defaults are the values the
+// schedule sweep chose on GB300 (fastlem_gb300/schedule.json); FL_LOW_ILP,
+// FL_WALK_PER_SM and FL_KAHN_MIN_WIDTH override them from the environment at load, and
+// fl_set_tuning at run time.
+struct Tuning {
+    int low_ilp = 4;              // top-down rounds: sites in flight per thread (1, 2 or 4)
+    uint32_t walk_per_sm = 0;     // chain walker blocks per SM; 0: as many as fit
+    uint32_t kahn_min_width = 0;  // Kahn rounds stop below this frontier width; 0: n / 512
+                                  // clamped to [8192, 65536]
+};
+Tuning& tuning();
+
 // Largest skeleton chain count whose walk kernels are all co-resident on the
-// current device (one warp per chain).
+// current device (one warp per chain), and the walkers' grid (blocks of kWalkWarps
+// warps) for the current tuning.
 uint32_t walk_capacity();
+uint32_t walk_grid();
 
 // Device-side bookkeeping words of one basin pass (uint32 slots of BasinArgs::meta).
 enum Meta {

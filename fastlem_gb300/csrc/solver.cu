@@ -64,17 +64,9 @@ constexpr uint32_t kKahnMinWidthLow = 8192;
 constexpr uint32_t kKahnMinWidthEarly = 8192;
 constexpr uint32_t kEarlyPasses = 2;
 
-// The stop width for a model of n sites, or FL_KAHN_MIN_WIDTH from the environment (a
-// tuning knob, read once).
+// The stop width for a model of n sites (the tuning's fixed width when it has one).
 uint32_t kahn_min_width(uint32_t n) {
-    static const uint32_t forced = [] {
-        if (const char* env = std::getenv("FL_KAHN_MIN_WIDTH")) {
-            const long v = std::strtol(env, nullptr, 10);
-            if (v >= 256 && v <= (1l << 24)) return (uint32_t)v;
-        }
-        return 0u;
-    }();
-    if (forced) return forced;
+    if (fl::tuning().kahn_min_width) return fl::tuning().kahn_min_width;
     return std::max(kKahnMinWidthLow, std::min(kKahnMinWidth, n / 512));
 }
 
@@ -319,6 +311,25 @@ unsigned coop_blocks(const void* kernel, unsigned block, unsigned cap_per_sm) {
 
 namespace fl {
 void set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+
+Tuning& tuning() {
+    static Tuning t = [] {
+        Tuning d;
+        auto env = [](const char* name, long lo, long hi, long dflt) {
+            if (const char* v = std::getenv(name)) {
+                const long x = std::strtol(v, nullptr, 10);
+                if (x >= lo && x <= hi) return x;
+            }
+            return dflt;
+        };
+        const long ilp = env("FL_LOW_ILP", 1, 4, d.low_ilp);
+        d.low_ilp = ilp >= 4 ? 4 : ilp >= 2 ? 2 : 1;
+        d.walk_per_sm = (uint32_t)env("FL_WALK_PER_SM", 0, 64, d.walk_per_sm);
+        d.kahn_min_width = (uint32_t)env("FL_KAHN_MIN_WIDTH", 256, 1l << 24, d.kahn_min_width);
+        return d;
+    }();
+    return t;
+}
 }  // namespace fl
 
 // ---------------------------------------------------------------------------
@@ -391,7 +402,6 @@ struct fl_graph {
     uint32_t *d_kslot = nullptr, *d_cpar = nullptr, *d_cqp = nullptr, *d_cdep = nullptr,
              *d_cpar1 = nullptr, *d_cdep1 = nullptr, *d_chist = nullptr, *d_corder = nullptr,
              *d_corder_up = nullptr;
-    uint32_t walk_grid = 0;
     fl::SlotRec* d_rec = nullptr;
     fl::SlotInfo* d_info = nullptr;
     uint32_t *d_tokslot = nullptr, *d_pend = nullptr;
@@ -508,7 +518,6 @@ int alloc_workspace(fl_graph* g) {
     const uint32_t n = g->n;
     // the Kahn rounds stop once fewer sites are ready than walk warps fit on the GPU
     g->kahn_min_width = kahn_min_width(n);
-    g->walk_grid = std::max<uint32_t>(1, fl::walk_capacity() / fl::kWalkWarps);
     FL_TRY(dalloc(&g->d_k, n));
     FL_TRY(dalloc(&g->d_u, n));
     FL_TRY(dalloc(&g->d_tan, n));
@@ -880,7 +889,7 @@ int enqueue_basin_pass(fl_graph* g, bool all_records = false) {
     a.chist = g->d_chist;
     a.corder = g->d_corder;
     a.corder_up = g->d_corder_up;
-    a.walk_grid = g->walk_grid;
+    a.walk_grid = fl::walk_grid();
     a.rec = g->d_rec;
     a.info = g->d_info;
     a.needl = g->d_needl;
@@ -1413,6 +1422,32 @@ int fl_graph_set_timing(fl_graph* g, int enable) {
 }
 
 uint64_t fl_graph_host_syncs(const fl_graph* g) { return g ? g->host_syncs : 0; }
+
+int fl_set_tuning(const char* name, int64_t value) {
+    g_err.clear();
+    fl::Tuning& t = fl::tuning();
+    const std::string k = name ? name : "";
+    if (k == "low_ilp" && (value == 1 || value == 2 || value == 4)) {
+        t.low_ilp = (int)value;
+    } else if (k == "walk_per_sm" && value >= 0 && value <= 64) {
+        t.walk_per_sm = (uint32_t)value;
+    } else if (k == "kahn_min_width" && (value == 0 || (value >= 256 && value <= (1 << 24)))) {
+        t.kahn_min_width = (uint32_t)value;
+    } else {
+        g_err = "fl_set_tuning: unknown name or value out of range";
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    return FL_OK;
+}
+
+int64_t fl_get_tuning(const char* name) {
+    const fl::Tuning& t = fl::tuning();
+    const std::string k = name ? name : "";
+    if (k == "low_ilp") return t.low_ilp;
+    if (k == "walk_per_sm") return t.walk_per_sm;
+    if (k == "kahn_min_width") return t.kahn_min_width;
+    return -1;
+}
 
 void fl_graph_reset_stats(fl_graph* g) {
     if (!g) return;

@@ -199,6 +199,19 @@ void fl_graph_reset_stats(fl_graph* g);
 /* Blocking host synchronisations the model's calls made since the last reset: one per
  * iteration of generate(), one more in an iteration that computes the lake order. */
 uint64_t fl_graph_host_syncs(const fl_graph* g);
+
+/* Launch shapes and switch points of the solve (no counterpart in the reference; the
+ * results are the same bits whatever they are):
+ *   "low_ilp"        top-down Kahn rounds, sites in flight per thread: 1, 2 or 4
+ *   "walk_per_sm"    chain walker blocks per SM, 1 .. 64 (at most what fits), 0: all that fit
+ *   "kahn_min_width" Kahn rounds stop below this frontier width (where the chain walks
+ *                    take over), 256 .. 2^24, or 0 for the default rule (n / 512 clamped
+ *                    to [8192, 65536]); applies to models created afterwards
+ * Process-wide; change them only while no solve runs.  The defaults are the committed
+ * schedule's (fastlem_gb300/schedule.json); FL_LOW_ILP, FL_WALK_PER_SM and
+ * FL_KAHN_MIN_WIDTH in the environment override them at load. */
+int fl_set_tuning(const char* name, int64_t value);
+int64_t fl_get_tuning(const char* name);   /* -1 for an unknown name */
 uint32_t fl_num_kernel_classes(void);
 int fl_graph_kernel_stats(const fl_graph* g, uint32_t cls, const char** name, uint64_t* launches,
                           double* device_ms, double* bytes);
