@@ -233,9 +233,12 @@ def cold_call(w, iters):
     gen = TerrainGenerator.default().set_model(fresh).set_parameters(w.params).set_max_iteration(iters)
     gen.generate()
     t2 = time.perf_counter()
+    from fastlem_gb300 import _lib
+    rank_ms, rank_where = _lib.rank_info(fresh.handle())
     fresh.release()
     return {"graph_create_s": t1 - t0, "first_generate_s": t2 - t1, "total_s": t2 - t0,
             "iterations": gen.last_iterations,
+            "lake_order": {"ms": rank_ms, "computed_on": rank_where},
             "what": "fl_graph_create + first fl_generate (lake order included), pageable "
                     "host arrays, host wall clock"}
 

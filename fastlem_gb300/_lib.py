@@ -29,7 +29,7 @@ EXPORTS = [
     "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_graph_host_syncs", "fl_set_tuning",
-    "fl_get_tuning", "fl_num_kernel_classes",
+    "fl_get_tuning", "fl_graph_rank_info", "fl_probe_lake_rank_gpu", "fl_num_kernel_classes",
     "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
     "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate", "fl_graph_device_bytes",
@@ -104,6 +104,8 @@ def lib():
     L.fl_set_tuning.argtypes = [ctypes.c_char_p, ctypes.c_int64]
     L.fl_get_tuning.argtypes = [ctypes.c_char_p]
     L.fl_get_tuning.restype = ctypes.c_int64
+    L.fl_graph_rank_info.argtypes = [vp, P(c_dbl), P(c_int)]
+    L.fl_probe_lake_rank_gpu.argtypes = [vp, vp, c_u32, vp, P(c_int)]
     L.fl_num_kernel_classes.restype = c_u32
     L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
     L.fl_graph_basin_stats.argtypes = [vp, vp, c_u32]
@@ -195,7 +197,7 @@ def kernel_stats(handle):
     return out
 
 
-TUNING = ("low_ilp", "walk_per_sm", "kahn_min_width")
+TUNING = ("low_ilp", "walk_per_sm", "gpu_rank", "kahn_min_width")
 
 
 def set_tuning(**kw):
@@ -212,6 +214,15 @@ def set_tuning(**kw):
 def get_tuning():
     L = lib()
     return {k: int(L.fl_get_tuning(k.encode())) for k in TUNING}
+
+
+def rank_info(handle):
+    """(ms, where) of the model's last lake-order computation: where is "gpu", "host" or
+    None."""
+    ms = c_dbl()
+    on = c_int()
+    check(lib().fl_graph_rank_info(handle, ctypes.byref(ms), ctypes.byref(on)))
+    return ms.value, {1: "gpu", 0: "host"}.get(on.value)
 
 
 def host_syncs(handle):

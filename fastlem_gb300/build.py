@@ -21,7 +21,7 @@ OUT_DIR = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(OUT_DIR, "libfastlem_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CUDA_SOURCES = ["solver.cu", "receivers.cu", "basin.cu", "noalloc.cu"]
+CUDA_SOURCES = ["solver.cu", "receivers.cu", "basin.cu", "noalloc.cu", "lake_rank.cu"]
 CXX_SOURCES = ["builder.cpp", "prim_rank.cpp", "ordering.cpp", "server.cpp", "interp.cpp"]
 HEADERS = ["rng.h", "common.cuh", "kernels.h", "fold.cuh", "delaunay.h"]
 

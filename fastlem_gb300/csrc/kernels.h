@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace fl {
 
 // Kernel classes for launch counting and per-class device timing.
@@ -33,6 +35,7 @@ struct Tuning {
     uint32_t walk_per_sm = 0;     // chain walker blocks per SM; 0: as many as fit
     uint32_t kahn_min_width = 0;  // Kahn rounds stop below this frontier width; 0: n / 512
                                   // clamped to [8192, 65536]
+    bool gpu_rank = true;         // the lake heap's order on the GPU where keys decide it
 };
 Tuning& tuning();
 
@@ -196,6 +199,20 @@ void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const ui
                       const uint8_t* outlet, uint32_t* next, double* rlen, int* flags);
 // ilen[s] = 1/len[s] in f32 (NaN where not a normal f32), for launch_receivers.
 void launch_inv_len(cudaStream_t st, uint64_t nnz, const double* len, float* ilen);
+
+// The lake heap's order on the GPU (lake_rank.cu): rank[v] (device order) and
+// sor[rank] = site, from the tied prefix the host replayed (the sites processed while
+// the smallest key is 0.0, in order).  kRankFallback: equal lengths could let the heap's
+// arrangement decide, or some length is not positive -- the host heap must be used.
+enum RankResult { kRankOk = 0, kRankFallback = 1, kRankError = 2 };
+struct GpuRankInfo {
+    cudaError_t error = cudaSuccess;
+    const char* fallback_reason = "";
+    uint32_t boruvka_rounds = 0, tree_edges = 0, lift_levels = 0, host_syncs = 0;
+};
+RankResult gpu_lake_rank(cudaStream_t st, uint32_t n, const uint32_t* row, const uint32_t* col,
+                         const double* len, uint64_t nnz, const std::vector<uint32_t>& prefix,
+                         uint32_t* rank, uint32_t* sor, GpuRankInfo* info);
 
 // Runs the exact parallel fold over one chain of n operands starting at x0 (probe).
 cudaError_t fold_probe(const double* y, uint32_t n, double x0, double* out);

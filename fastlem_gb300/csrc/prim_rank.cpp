@@ -233,6 +233,31 @@ bool keyed_rank(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const 
 
 }  // namespace
 
+// The tied prefix of the traversal: the sites the reference's heap processes while the
+// smallest queued key is 0.0 (the outlets, in the order its arrangement gives them, and
+// any site reached over a zero-length edge), in processing order.  With every edge
+// longer than zero the rest of the order is decided by keys alone (the GPU rank).
+// Returns false when a NaN key was pushed.
+bool lake_rank_prefix(uint32_t n, const uint32_t* row_ptr, const uint32_t* col,
+                      const double* len, const uint32_t* outlets, uint32_t n_out,
+                      std::vector<uint32_t>& order) {
+    LakeHeap heap((size_t)n_out + 64);
+    std::vector<uint8_t> visited(n, 0);
+    order.clear();
+    for (uint32_t o = 0; o < n_out; ++o) heap.push(outlets[o], 0.0);
+    while (!heap.empty() && heap.top_key() == 0.0) {
+        uint32_t i = heap.pop();
+        if (visited[i]) continue;
+        for (uint32_t s = row_ptr[i]; s < row_ptr[i + 1]; ++s) {
+            uint32_t j = col[s];
+            if (!visited[j]) heap.push(j, len[s]);
+        }
+        visited[i] = 1;
+        order.push_back(i);
+    }
+    return !heap.nan_seen();
+}
+
 // rank[v] = index of v in the processing order, UINT32_MAX for sites the traversal
 // never reaches.  Returns false when a NaN key was pushed (the reference panics).
 bool lake_heap_rank(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,

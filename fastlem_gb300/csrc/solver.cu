@@ -37,6 +37,9 @@
 namespace fl {
 bool lake_heap_rank(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
                     const uint32_t* outlets, uint32_t n_out, uint32_t* rank);
+bool lake_rank_prefix(uint32_t n, const uint32_t* row_ptr, const uint32_t* col,
+                      const double* len, const uint32_t* outlets, uint32_t n_out,
+                      std::vector<uint32_t>& order);
 void hilbert_order(uint32_t n, const double* xs, const double* ys, std::vector<uint32_t>& perm);
 void relabel_csr(uint32_t n, const uint32_t* row, const uint32_t* col, const double* len,
                  const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
@@ -326,6 +329,7 @@ Tuning& tuning() {
         d.low_ilp = ilp >= 4 ? 4 : ilp >= 2 ? 2 : 1;
         d.walk_per_sm = (uint32_t)env("FL_WALK_PER_SM", 0, 64, d.walk_per_sm);
         d.kahn_min_width = (uint32_t)env("FL_KAHN_MIN_WIDTH", 256, 1l << 24, d.kahn_min_width);
+        d.gpu_rank = env("FL_GPU_RANK", 0, 1, d.gpu_rank) != 0;
         return d;
     }();
     return t;
@@ -354,7 +358,9 @@ struct fl_graph {
     std::vector<uint32_t> rank_key;
     bool rank_valid = false;
     bool rank_uploaded = false;
-    std::vector<uint32_t> h_rank;
+    std::vector<uint32_t> h_rank;        // host-computed rank (empty when computed on the GPU)
+    int rank_gpu = -1;                   // where the last rank was computed: 1 GPU, 0 host
+    double rank_ms = 0.0;                // its host wall time
     // device order: perm[device index] = caller index, inv the reverse
     std::vector<uint32_t> perm, inv;
     uint32_t *d_perm = nullptr, *d_inv = nullptr;
@@ -708,8 +714,36 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
         g->rank_uploaded = false;
         g->rank_key = outlets;
     }
+    if (need_rank && !g->rank_uploaded && g->terrains == 1 && fl::tuning().gpu_rank) {
+        // the keyed order on the GPU after the tied prefix replayed here; the host heap
+        // when equal or non-positive lengths could let its arrangement decide
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<uint32_t> prefix;
+        if (!fl::lake_rank_prefix(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
+                                  outlets.data(), (uint32_t)outlets.size(), prefix)) {
+            g_err = "NaN edge length in the lake traversal";
+            return FL_ERR_INVALID_ARGUMENT;
+        }
+        fl::GpuRankInfo info;
+        const fl::RankResult r = fl::gpu_lake_rank(g->stream, n, g->d_row, g->d_col, g->d_len,
+                                                   g->nnz, prefix, g->d_rank, g->d_sor, &info);
+        if (r == fl::kRankError) {
+            set_err("lake order on the GPU", info.error);
+            return FL_ERR_CUDA;
+        }
+        if (r == fl::kRankOk) {
+            FL_CU(cudaStreamSynchronize(g->stream));
+            g->h_rank.clear();
+            g->rank_valid = g->rank_uploaded = true;
+            g->rank_gpu = 1;
+            g->rank_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            return FL_OK;
+        }
+        g->rank_gpu = 0;                              // fall through to the host heap
+    }
     if (need_rank && !g->rank_uploaded) {
-        if (!g->rank_valid) {
+        const auto t0 = std::chrono::steady_clock::now();
+        if (!g->rank_valid || g->h_rank.size() != n) {
             g->h_rank.resize(n);
             if (g->terrains == 1) {
                 if (!fl::lake_heap_rank(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
@@ -751,6 +785,8 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
         FL_CU(cudaMemcpyAsync(g->d_sor, sor.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
         FL_CU(cudaStreamSynchronize(g->stream));
         g->rank_uploaded = true;
+        g->rank_gpu = 0;
+        g->rank_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     return FL_OK;
 }
@@ -1431,6 +1467,8 @@ int fl_set_tuning(const char* name, int64_t value) {
         t.low_ilp = (int)value;
     } else if (k == "walk_per_sm" && value >= 0 && value <= 64) {
         t.walk_per_sm = (uint32_t)value;
+    } else if (k == "gpu_rank" && (value == 0 || value == 1)) {
+        t.gpu_rank = value != 0;
     } else if (k == "kahn_min_width" && (value == 0 || (value >= 256 && value <= (1 << 24)))) {
         t.kahn_min_width = (uint32_t)value;
     } else {
@@ -1446,7 +1484,50 @@ int64_t fl_get_tuning(const char* name) {
     if (k == "low_ilp") return t.low_ilp;
     if (k == "walk_per_sm") return t.walk_per_sm;
     if (k == "kahn_min_width") return t.kahn_min_width;
+    if (k == "gpu_rank") return t.gpu_rank ? 1 : 0;
     return -1;
+}
+
+int fl_graph_rank_info(const fl_graph* g, double* ms, int* on_gpu) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    if (ms) *ms = g->rank_ms;
+    if (on_gpu) *on_gpu = g->rank_gpu;
+    return FL_OK;
+}
+
+int fl_probe_lake_rank_gpu(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
+                           uint32_t* rank, int* used_gpu) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    if (!rank || (n_outlets && !outlets)) return FL_ERR_INVALID_ARGUMENT;
+    FL_CU(cudaSetDevice(g->device));
+    const uint32_t n = g->n;
+    for (uint32_t i = 0; i < n_outlets; ++i)
+        if (outlets[i] >= n) return FL_ERR_INVALID_ARGUMENT;
+    std::vector<uint32_t> o = to_device_ids(g, outlets, n_outlets), prefix;
+    if (!fl::lake_rank_prefix(n, g->h_row.data(), g->h_col.data(), g->h_len.data(), o.data(),
+                              n_outlets, prefix)) {
+        g_err = "NaN edge length in the lake traversal";
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    // into the solver's rank arrays: the next lake pass recomputes its own order
+    g->rank_valid = g->rank_uploaded = false;
+    fl::GpuRankInfo info;
+    const fl::RankResult r = fl::gpu_lake_rank(g->stream, n, g->d_row, g->d_col, g->d_len, g->nnz,
+                                               prefix, g->d_rank, g->d_sor, &info);
+    if (r == fl::kRankError) {
+        set_err("lake order on the GPU", info.error);
+        return FL_ERR_CUDA;
+    }
+    if (used_gpu) *used_gpu = r == fl::kRankOk ? 1 : 0;
+    if (r == fl::kRankFallback) {
+        g_err = info.fallback_reason;
+        return FL_OK;
+    }
+    std::vector<uint32_t> dr(n);
+    FL_CU(cudaMemcpyAsync(dr.data(), g->d_rank, n * 4ull, cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaStreamSynchronize(g->stream));
+    for (uint32_t i = 0; i < n; ++i) rank[i] = dr[g->inv[i]];
+    return FL_OK;
 }
 
 void fl_graph_reset_stats(fl_graph* g) {

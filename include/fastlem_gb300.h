@@ -204,14 +204,20 @@ uint64_t fl_graph_host_syncs(const fl_graph* g);
  * results are the same bits whatever they are):
  *   "low_ilp"        top-down Kahn rounds, sites in flight per thread: 1, 2 or 4
  *   "walk_per_sm"    chain walker blocks per SM, 1 .. 64 (at most what fits), 0: all that fit
+ *   "gpu_rank"       1: the lake heap's order computed on the GPU where lengths decide it
+ *                    (the host heap otherwise), 0: always the host heap
  *   "kahn_min_width" Kahn rounds stop below this frontier width (where the chain walks
  *                    take over), 256 .. 2^24, or 0 for the default rule (n / 512 clamped
  *                    to [8192, 65536]); applies to models created afterwards
  * Process-wide; change them only while no solve runs.  The defaults are the committed
- * schedule's (fastlem_gb300/schedule.json); FL_LOW_ILP, FL_WALK_PER_SM and
- * FL_KAHN_MIN_WIDTH in the environment override them at load. */
+ * schedule's (fastlem_gb300/schedule.json); FL_LOW_ILP, FL_WALK_PER_SM, FL_GPU_RANK
+ * and FL_KAHN_MIN_WIDTH in the environment override them at load. */
 int fl_set_tuning(const char* name, int64_t value);
 int64_t fl_get_tuning(const char* name);   /* -1 for an unknown name */
+
+/* Where and how long the model's last lake-order computation ran: *on_gpu 1 (GPU), 0
+ * (host heap) or -1 (none yet); *ms its host wall time. */
+int fl_graph_rank_info(const fl_graph* g, double* ms, int* on_gpu);
 uint32_t fl_num_kernel_classes(void);
 int fl_graph_kernel_stats(const fl_graph* g, uint32_t cls, const char** name, uint64_t* launches,
                           double* device_ms, double* bytes);
@@ -256,6 +262,14 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
 /* The order in which the reference's lake heap processes sites
  * (lem/stream_tree.rs:184-240), computed on the host: rank[v], UINT32_MAX if never. */
 int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets, uint32_t* rank);
+
+/* The same order computed on the GPU (caller's site order): the outlets' tied prefix
+ * replayed on the host, then the keyed part from the minimum spanning tree.  *used_gpu
+ * is 0 when equal or non-positive lengths could let the heap's arrangement decide (rank
+ * is then left untouched and fl_last_error says why).  Replaces the model's cached lake
+ * order. */
+int fl_probe_lake_rank_gpu(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
+                           uint32_t* rank, int* used_gpu);
 
 /* x_k = (...((start + op_0) + op_1) ... + op_k) with every addition rounded, as the
  * reference's sequential accumulations do, evaluated by the solver's parallel exact
