@@ -29,7 +29,8 @@ EXPORTS = [
     "fl_graph_create", "fl_graph_destroy", "fl_generate", "fl_generate_timed",
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_graph_host_syncs", "fl_set_tuning",
-    "fl_get_tuning", "fl_graph_rank_info", "fl_probe_lake_rank_gpu", "fl_num_kernel_classes",
+    "fl_get_tuning", "fl_graph_rank_info", "fl_probe_lake_rank_gpu",
+    "fl_schedule_entry", "fl_num_kernel_classes",
     "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
     "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate", "fl_graph_device_bytes",
@@ -105,6 +106,7 @@ def lib():
     L.fl_get_tuning.argtypes = [ctypes.c_char_p]
     L.fl_get_tuning.restype = ctypes.c_int64
     L.fl_graph_rank_info.argtypes = [vp, P(c_dbl), P(c_int)]
+    L.fl_schedule_entry.argtypes = [c_u32, P(c_u32), P(c_int), P(c_int), P(c_u32), P(c_u32)]
     L.fl_probe_lake_rank_gpu.argtypes = [vp, vp, c_u32, vp, P(c_int)]
     L.fl_num_kernel_classes.restype = c_u32
     L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
@@ -209,6 +211,19 @@ def set_tuning(**kw):
         old[k] = int(L.fl_get_tuning(k.encode()))
         check(L.fl_set_tuning(k.encode(), int(v)))
     return old
+
+
+def schedule():
+    """The library's compiled-in schedule: [(max_sites, packed, low_ilp, walk_per_sm,
+    kahn_min_width)]."""
+    out = []
+    i = 0
+    while True:
+        v = [c_u32(), c_int(), c_int(), c_u32(), c_u32()]
+        if lib().fl_schedule_entry(i, *[ctypes.byref(x) for x in v]) != FL_OK:
+            return out
+        out.append(tuple(int(x.value) for x in v))
+        i += 1
 
 
 def get_tuning():

@@ -1509,11 +1509,10 @@ uint32_t walk_capacity() {
     return (uint32_t)(sms * per * kWalkWarps);
 }
 
-uint32_t walk_grid() {
+uint32_t walk_grid(uint32_t per_sm) {
     static uint32_t cached = 0;            // the GPUs of a process match
     if (!cached) cached = std::max<uint32_t>(1, walk_capacity() / kWalkWarps);
     uint32_t g = cached;
-    const uint32_t per_sm = tuning().walk_per_sm;
     if (per_sm) {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
@@ -1647,7 +1646,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     // parent t/elev/bas 20, outlet t/elev 16 per site
     hk.begin(hk.ctx);
     {
-        const int K = tuning().low_ilp;
+        const int K = a.low_ilp;
         const void* kern =
             a.slope ? (K == 4 ? (const void*)k_low_top_down<true, 4>
                               : K == 2 ? (const void*)k_low_top_down<true, 2>

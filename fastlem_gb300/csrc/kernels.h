@@ -26,24 +26,39 @@ enum KClass {
 // Skeleton chains are walked one warp each, this many warps per block.
 constexpr int kWalkWarps = 4;
 
-// Tunable launch shapes and switch points, process-wide.  Defaults are the values the
-// schedule sweep chose on GB300 (fastlem_gb300/schedule.json); FL_LOW_ILP,
-// FL_WALK_PER_SM and FL_KAHN_MIN_WIDTH override them from the environment at load, and
+// Launch shapes and switch points of one model's solve.
+struct Shape {
+    int low_ilp;              // top-down Kahn rounds: sites in flight per thread (1, 2 or 4)
+    uint32_t walk_per_sm;     // chain walker blocks per SM; 0: as many as fit
+    uint32_t kahn_min_width;  // Kahn rounds stop below this frontier width; 0: n / 512
+                              // clamped to [8192, 65536]
+};
+// The schedule: per size class (models of up to max_sites sites; packed batches apart)
+// the shapes the schedule sweep chose on GB300 (fastlem_gb300/schedule.json).
+struct ScheduleEntry {
+    uint32_t max_sites;
+    bool packed;
+    Shape shape;
+};
+const std::vector<ScheduleEntry>& schedule();
+// Process-wide overrides of the schedule (-1: none) and the GPU lake-order switch;
+// FL_LOW_ILP, FL_WALK_PER_SM, FL_KAHN_MIN_WIDTH and FL_GPU_RANK set them at load,
 // fl_set_tuning at run time.
 struct Tuning {
-    int low_ilp = 4;              // top-down rounds: sites in flight per thread (1, 2 or 4)
-    uint32_t walk_per_sm = 0;     // chain walker blocks per SM; 0: as many as fit
-    uint32_t kahn_min_width = 0;  // Kahn rounds stop below this frontier width; 0: n / 512
-                                  // clamped to [8192, 65536]
-    bool gpu_rank = true;         // the lake heap's order on the GPU where keys decide it
+    int low_ilp = -1;
+    int walk_per_sm = -1;
+    int64_t kahn_min_width = -1;
+    bool gpu_rank = true;
 };
 Tuning& tuning();
+// The shapes for a model of n sites (packed: several terrains), overrides applied.
+Shape shape_for(uint32_t n, bool packed);
 
 // Largest skeleton chain count whose walk kernels are all co-resident on the
 // current device (one warp per chain), and the walkers' grid (blocks of kWalkWarps
 // warps) for the current tuning.
 uint32_t walk_capacity();
-uint32_t walk_grid();
+uint32_t walk_grid(uint32_t per_sm);
 
 // Device-side bookkeeping words of one basin pass (uint32 slots of BasinArgs::meta).
 enum Meta {
@@ -163,6 +178,7 @@ struct BasinArgs {
     uint32_t* corder;       // chains by depth, shallowest first: the top-down claim order
     uint32_t* corder_up;    // chains by height, lowest first: the bottom-up claim order
     uint32_t walk_grid;     // blocks of the persistent chain walkers (all co-resident)
+    int low_ilp;            // top-down Kahn rounds: sites in flight per thread
     double* el;             // skeleton elevations in layout order (slope limits only)
     uint32_t* cbas;         // per chain: basin outlet, its response time and elevation
     double* cto;

@@ -67,9 +67,10 @@ constexpr uint32_t kKahnMinWidthLow = 8192;
 constexpr uint32_t kKahnMinWidthEarly = 8192;
 constexpr uint32_t kEarlyPasses = 2;
 
-// The stop width for a model of n sites (the tuning's fixed width when it has one).
-uint32_t kahn_min_width(uint32_t n) {
-    if (fl::tuning().kahn_min_width) return fl::tuning().kahn_min_width;
+// The stop width for a model of n sites (packed: several terrains).
+uint32_t kahn_min_width(uint32_t n, bool packed = false) {
+    const uint32_t w = fl::shape_for(n, packed).kahn_min_width;
+    if (w) return w;
     return std::max(kKahnMinWidthLow, std::min(kKahnMinWidth, n / 512));
 }
 
@@ -325,14 +326,39 @@ Tuning& tuning() {
             }
             return dflt;
         };
-        const long ilp = env("FL_LOW_ILP", 1, 4, d.low_ilp);
-        d.low_ilp = ilp >= 4 ? 4 : ilp >= 2 ? 2 : 1;
-        d.walk_per_sm = (uint32_t)env("FL_WALK_PER_SM", 0, 64, d.walk_per_sm);
-        d.kahn_min_width = (uint32_t)env("FL_KAHN_MIN_WIDTH", 256, 1l << 24, d.kahn_min_width);
-        d.gpu_rank = env("FL_GPU_RANK", 0, 1, d.gpu_rank) != 0;
+        const long ilp = env("FL_LOW_ILP", 1, 4, -1);
+        d.low_ilp = ilp < 0 ? -1 : ilp >= 4 ? 4 : ilp >= 2 ? 2 : 1;
+        d.walk_per_sm = (int)env("FL_WALK_PER_SM", 0, 64, -1);
+        d.kahn_min_width = env("FL_KAHN_MIN_WIDTH", 256, 1l << 24, -1);
+        d.gpu_rank = env("FL_GPU_RANK", 0, 1, 1) != 0;
         return d;
     }();
     return t;
+}
+
+// The committed schedule (fastlem_gb300/schedule.json, written by the schedule sweep
+// fastlem_gb300/autotune.py); a CPU test keeps the two equal.
+const std::vector<ScheduleEntry>& schedule() {
+    static const std::vector<ScheduleEntry> s = {
+        // max_sites, packed, {low_ilp, walk_per_sm, kahn_min_width}
+        {0xffffffffu, false, {4, 0, 0}},
+        {0xffffffffu, true, {4, 0, 0}},
+    };
+    return s;
+}
+
+Shape shape_for(uint32_t n, bool packed) {
+    Shape sh{4, 0, 0};
+    for (const ScheduleEntry& e : schedule())
+        if (e.packed == packed && n <= e.max_sites) {
+            sh = e.shape;
+            break;
+        }
+    const Tuning& t = tuning();
+    if (t.low_ilp > 0) sh.low_ilp = t.low_ilp;
+    if (t.walk_per_sm >= 0) sh.walk_per_sm = (uint32_t)t.walk_per_sm;
+    if (t.kahn_min_width >= 0) sh.kahn_min_width = (uint32_t)t.kahn_min_width;
+    return sh;
 }
 }  // namespace fl
 
@@ -523,7 +549,7 @@ void kresolve(fl_graph* g) {
 int alloc_workspace(fl_graph* g) {
     const uint32_t n = g->n;
     // the Kahn rounds stop once fewer sites are ready than walk warps fit on the GPU
-    g->kahn_min_width = kahn_min_width(n);
+    g->kahn_min_width = kahn_min_width(n, g->terrains > 1);
     FL_TRY(dalloc(&g->d_k, n));
     FL_TRY(dalloc(&g->d_u, n));
     FL_TRY(dalloc(&g->d_tan, n));
@@ -714,15 +740,39 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
         g->rank_uploaded = false;
         g->rank_key = outlets;
     }
-    if (need_rank && !g->rank_uploaded && g->terrains == 1 && fl::tuning().gpu_rank) {
+    if (need_rank && !g->rank_uploaded && fl::tuning().gpu_rank) {
         // the keyed order on the GPU after the tied prefix replayed here; the host heap
-        // when equal or non-positive lengths could let its arrangement decide
+        // when equal or non-positive lengths could let its arrangement decide.  Packed
+        // terrains: each terrain's own prefix (its own heap), concatenated; one contracted
+        // source for all of them keeps every terrain's order (a terrain's frontier only
+        // moves by its own pops), and lakes compare ranks within their terrain only.
         const auto t0 = std::chrono::steady_clock::now();
         std::vector<uint32_t> prefix;
-        if (!fl::lake_rank_prefix(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
-                                  outlets.data(), (uint32_t)outlets.size(), prefix)) {
-            g_err = "NaN edge length in the lake traversal";
-            return FL_ERR_INVALID_ARGUMENT;
+        if (g->terrains == 1) {
+            if (!fl::lake_rank_prefix(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
+                                      outlets.data(), (uint32_t)outlets.size(), prefix)) {
+                g_err = "NaN edge length in the lake traversal";
+                return FL_ERR_INVALID_ARGUMENT;
+            }
+        } else {
+            std::vector<uint32_t> lrow, lcol, lout, lpre;
+            size_t oi = 0;
+            for (uint32_t t = 0; t < g->terrains; ++t) {
+                const uint32_t a = g->site_off[t], b = g->site_off[t + 1], m = b - a;
+                const uint32_t s0 = g->h_row[a];
+                lrow.resize(m + 1);
+                for (uint32_t j = 0; j <= m; ++j) lrow[j] = g->h_row[a + j] - s0;
+                lcol.resize(g->h_row[b] - s0);
+                for (uint32_t s = s0; s < g->h_row[b]; ++s) lcol[s - s0] = g->h_col[s] - a;
+                lout.clear();
+                while (oi < outlets.size() && outlets[oi] < b) lout.push_back(outlets[oi++] - a);
+                if (!fl::lake_rank_prefix(m, lrow.data(), lcol.data(), g->h_len.data() + s0,
+                                          lout.data(), (uint32_t)lout.size(), lpre)) {
+                    g_err = "NaN edge length in the lake traversal";
+                    return FL_ERR_INVALID_ARGUMENT;
+                }
+                for (uint32_t v : lpre) prefix.push_back(a + v);
+            }
         }
         fl::GpuRankInfo info;
         const fl::RankResult r = fl::gpu_lake_rank(g->stream, n, g->d_row, g->d_col, g->d_len,
@@ -925,7 +975,9 @@ int enqueue_basin_pass(fl_graph* g, bool all_records = false) {
     a.chist = g->d_chist;
     a.corder = g->d_corder;
     a.corder_up = g->d_corder_up;
-    a.walk_grid = fl::walk_grid();
+    const fl::Shape sh = fl::shape_for(g->n, g->terrains > 1);
+    a.walk_grid = fl::walk_grid(sh.walk_per_sm);
+    a.low_ilp = sh.low_ilp;
     a.rec = g->d_rec;
     a.info = g->d_info;
     a.needl = g->d_needl;
@@ -1463,14 +1515,15 @@ int fl_set_tuning(const char* name, int64_t value) {
     g_err.clear();
     fl::Tuning& t = fl::tuning();
     const std::string k = name ? name : "";
-    if (k == "low_ilp" && (value == 1 || value == 2 || value == 4)) {
+    if (k == "low_ilp" && (value == -1 || value == 1 || value == 2 || value == 4)) {
         t.low_ilp = (int)value;
-    } else if (k == "walk_per_sm" && value >= 0 && value <= 64) {
-        t.walk_per_sm = (uint32_t)value;
+    } else if (k == "walk_per_sm" && value >= -1 && value <= 64) {
+        t.walk_per_sm = (int)value;
     } else if (k == "gpu_rank" && (value == 0 || value == 1)) {
         t.gpu_rank = value != 0;
-    } else if (k == "kahn_min_width" && (value == 0 || (value >= 256 && value <= (1 << 24)))) {
-        t.kahn_min_width = (uint32_t)value;
+    } else if (k == "kahn_min_width" &&
+               (value == -1 || value == 0 || (value >= 256 && value <= (1 << 24)))) {
+        t.kahn_min_width = value;
     } else {
         g_err = "fl_set_tuning: unknown name or value out of range";
         return FL_ERR_INVALID_ARGUMENT;
@@ -1485,7 +1538,19 @@ int64_t fl_get_tuning(const char* name) {
     if (k == "walk_per_sm") return t.walk_per_sm;
     if (k == "kahn_min_width") return t.kahn_min_width;
     if (k == "gpu_rank") return t.gpu_rank ? 1 : 0;
-    return -1;
+    return -2;
+}
+
+int fl_schedule_entry(uint32_t i, uint32_t* max_sites, int* packed, int* low_ilp,
+                      uint32_t* walk_per_sm, uint32_t* kahn_min_width) {
+    const auto& s = fl::schedule();
+    if (i >= s.size()) return FL_ERR_INVALID_ARGUMENT;
+    if (max_sites) *max_sites = s[i].max_sites;
+    if (packed) *packed = s[i].packed ? 1 : 0;
+    if (low_ilp) *low_ilp = s[i].shape.low_ilp;
+    if (walk_per_sm) *walk_per_sm = s[i].shape.walk_per_sm;
+    if (kahn_min_width) *kahn_min_width = s[i].shape.kahn_min_width;
+    return FL_OK;
 }
 
 int fl_graph_rank_info(const fl_graph* g, double* ms, int* on_gpu) {

@@ -201,19 +201,25 @@ void fl_graph_reset_stats(fl_graph* g);
 uint64_t fl_graph_host_syncs(const fl_graph* g);
 
 /* Launch shapes and switch points of the solve (no counterpart in the reference; the
- * results are the same bits whatever they are):
+ * results are the same bits whatever they are).  By default each model takes the
+ * committed schedule's shapes for its size class (fastlem_gb300/schedule.json, listed by
+ * fl_schedule_entry); fl_set_tuning overrides them process-wide, -1 restoring the
+ * schedule:
  *   "low_ilp"        top-down Kahn rounds, sites in flight per thread: 1, 2 or 4
  *   "walk_per_sm"    chain walker blocks per SM, 1 .. 64 (at most what fits), 0: all that fit
+ *   "kahn_min_width" Kahn rounds stop below this frontier width (where the chain walks
+ *                    take over), 256 .. 2^24, or 0 for n / 512 clamped to [8192, 65536];
+ *                    read when a model is created
  *   "gpu_rank"       1: the lake heap's order computed on the GPU where lengths decide it
  *                    (the host heap otherwise), 0: always the host heap
- *   "kahn_min_width" Kahn rounds stop below this frontier width (where the chain walks
- *                    take over), 256 .. 2^24, or 0 for the default rule (n / 512 clamped
- *                    to [8192, 65536]); applies to models created afterwards
- * Process-wide; change them only while no solve runs.  The defaults are the committed
- * schedule's (fastlem_gb300/schedule.json); FL_LOW_ILP, FL_WALK_PER_SM, FL_GPU_RANK
- * and FL_KAHN_MIN_WIDTH in the environment override them at load. */
+ * Change them only while no solve runs.  FL_LOW_ILP, FL_WALK_PER_SM, FL_KAHN_MIN_WIDTH and
+ * FL_GPU_RANK in the environment set them at load. */
 int fl_set_tuning(const char* name, int64_t value);
-int64_t fl_get_tuning(const char* name);   /* -1 for an unknown name */
+int64_t fl_get_tuning(const char* name);   /* -2 for an unknown name */
+/* Schedule entry i (FL_ERR_INVALID_ARGUMENT past the end): models of up to max_sites
+ * sites (packed batches when packed is 1) use these shapes; 0 width = the n / 512 rule. */
+int fl_schedule_entry(uint32_t i, uint32_t* max_sites, int* packed, int* low_ilp,
+                      uint32_t* walk_per_sm, uint32_t* kahn_min_width);
 
 /* Where and how long the model's last lake-order computation ran: *on_gpu 1 (GPU), 0
  * (host heap) or -1 (none yet); *ms its host wall time. */
