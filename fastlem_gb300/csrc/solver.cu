@@ -341,8 +341,12 @@ Tuning& tuning() {
 const std::vector<ScheduleEntry>& schedule() {
     static const std::vector<ScheduleEntry> s = {
         // max_sites, packed, {low_ilp, walk_per_sm, kahn_min_width}
-        {0xffffffffu, false, {4, 0, 0}},
-        {0xffffffffu, true, {4, 0, 0}},
+        {0x20000u, false, {4, 4, 2048}},
+        {0x80000u, false, {4, 4, 2048}},
+        {0x200000u, false, {4, 0, 4096}},
+        {0x7d0000u, false, {4, 0, 4096}},
+        {0xffffffffu, false, {4, 4, 0}},
+        {0xffffffffu, true, {2, 0, 0}},
     };
     return s;
 }

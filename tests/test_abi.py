@@ -179,3 +179,18 @@ def test_graph_create_rejects_missing_arrays(fl_lib):
                                   None, ctypes.byref(h)) == FL_ERR_INVALID_ARGUMENT
     assert fl_lib.fl_graph_create(2, ptr(row_ptr), None, ptr(length), ptr(area), None, 0, None,
                                   None, ctypes.byref(h)) == FL_ERR_INVALID_ARGUMENT
+
+
+def test_compiled_schedule_is_the_committed_one(fl_lib):
+    """The library's compiled-in launch-shape schedule equals fastlem_gb300/schedule.json
+    (the schedule sweep's output), class for class."""
+    import json
+    import os
+    from fastlem_gb300 import _lib
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "fastlem_gb300", "schedule.json")
+    with open(path) as f:
+        classes = json.load(f)["classes"]
+    want = [(c["max_sites"], int(c["packed"]), c["best"]["low_ilp"], c["best"]["walk_per_sm"],
+             c["best"]["kahn_min_width"]) for c in classes]
+    assert _lib.schedule() == want
