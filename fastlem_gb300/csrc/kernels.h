@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
 #include <vector>
 
 namespace fl {
@@ -215,6 +216,36 @@ void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const ui
                       const uint8_t* outlet, uint32_t* next, double* rlen, int* flags);
 // ilen[s] = 1/len[s] in f32 (NaN where not a normal f32), for launch_receivers.
 void launch_inv_len(cudaStream_t st, uint64_t nnz, const double* len, float* ilen);
+
+// A model as the caller gives it (host arrays; site_off has terrains + 1 offsets) and
+// the device arrays ordering.cu fills in memory order (tid / noise_idx only for packed
+// terrains).
+struct GraphInput {
+    uint32_t n;
+    uint64_t nnz;
+    const uint32_t* row_ptr;
+    const uint32_t* col;
+    const double* len;
+    const double* area;
+    const double* xs;         // both null: caller order is kept
+    const double* ys;
+    uint32_t terrains;
+    const uint32_t* site_off;
+};
+struct GraphOutput {
+    uint32_t* row;
+    uint32_t* col;
+    double* len;
+    double* area;
+    uint32_t* perm;           // perm[device index] = caller index
+    uint32_t* inv;
+    uint32_t* tid;
+    uint32_t* noise_idx;
+};
+// Uploads, checks (0, or 20 with *err for invalid input, 21 / 22 for CUDA errors /
+// out of memory) and relabels; the arrays are ready when it returns.
+int build_device_graph(cudaStream_t st, const GraphInput& in, const GraphOutput& out,
+                       std::string* err);
 
 // The lake heap's order on the GPU (lake_rank.cu): rank[v] (device order) and
 // sor[rank] = site, from the tied prefix the host replayed (the sites processed while

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <unordered_map>
 #include <vector>
 
 #include "fastlem_gb300.h"
@@ -256,6 +257,43 @@ bool lake_rank_prefix(uint32_t n, const uint32_t* row_ptr, const uint32_t* col,
         order.push_back(i);
     }
     return !heap.nan_seen();
+}
+
+// The same tied prefix from the outlets' own rows only (row i of orow / ocol / olen
+// belongs to outlets[i], offsets absolute): with every edge longer than zero only
+// outlets are processed at key 0.0.  Returns 0, 1 when a NaN key was pushed, 2 when a
+// site that is not an outlet comes up at key 0.0 (a zero-length edge: the full graph
+// is needed).
+int lake_rank_prefix_rows(uint32_t n, const uint32_t* outlets, uint32_t n_out,
+                          const uint32_t* orow, const uint32_t* ocol, const double* olen,
+                          std::vector<uint32_t>& order) {
+    std::unordered_map<uint32_t, uint32_t> at;            // site -> its first list position
+    at.reserve(n_out * 2 + 1);
+    for (uint32_t o = 0; o < n_out; ++o) at.emplace(outlets[o], o);
+    // only outlets are processed here, so "visited" lives on their list positions
+    std::vector<uint8_t> done(n_out, 0);
+    auto visited = [&](uint32_t site) {
+        const auto it = at.find(site);
+        return it != at.end() && done[it->second];
+    };
+    (void)n;
+    LakeHeap heap((size_t)n_out + 64);
+    order.clear();
+    for (uint32_t o = 0; o < n_out; ++o) heap.push(outlets[o], 0.0);
+    while (!heap.empty() && heap.top_key() == 0.0) {
+        const uint32_t i = heap.pop();
+        const auto it = at.find(i);
+        if (it == at.end()) return 2;
+        const uint32_t p = it->second;
+        if (done[p]) continue;
+        for (uint32_t s = orow[p]; s < orow[p + 1]; ++s) {
+            const uint32_t j = ocol[s];
+            if (!visited(j)) heap.push(j, olen[s]);
+        }
+        done[p] = 1;
+        order.push_back(i);
+    }
+    return heap.nan_seen() ? 1 : 0;
 }
 
 // rank[v] = index of v in the processing order, UINT32_MAX for sites the traversal

@@ -37,13 +37,9 @@
 namespace fl {
 bool lake_heap_rank(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
                     const uint32_t* outlets, uint32_t n_out, uint32_t* rank);
-bool lake_rank_prefix(uint32_t n, const uint32_t* row_ptr, const uint32_t* col,
-                      const double* len, const uint32_t* outlets, uint32_t n_out,
-                      std::vector<uint32_t>& order);
-void hilbert_order(uint32_t n, const double* xs, const double* ys, std::vector<uint32_t>& perm);
-void relabel_csr(uint32_t n, const uint32_t* row, const uint32_t* col, const double* len,
-                 const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
-                 std::vector<uint32_t>& nrow, std::vector<uint32_t>& ncol, std::vector<double>& nlen);
+int lake_rank_prefix_rows(uint32_t n, const uint32_t* outlets, uint32_t n_out,
+                          const uint32_t* orow, const uint32_t* ocol, const double* olen,
+                          std::vector<uint32_t>& order);
 }
 
 namespace {
@@ -725,6 +721,110 @@ int download_permuted(fl_graph* g, const double* src, double* dst) {
     return FL_OK;
 }
 
+// The model's CSR (device order) on the host, for the host heap and the probes;
+// downloaded on first use.
+int ensure_host_csr(fl_graph* g) {
+    if (g->h_row.size() == g->n + 1ull) return FL_OK;
+    g->h_row.resize(g->n + 1ull);
+    g->h_col.resize(g->nnz);
+    g->h_len.resize(g->nnz);
+    FL_CU(cudaMemcpyAsync(g->h_row.data(), g->d_row, (g->n + 1ull) * 4, cudaMemcpyDeviceToHost, g->stream));
+    if (g->nnz) {
+        FL_CU(cudaMemcpyAsync(g->h_col.data(), g->d_col, g->nnz * 4, cudaMemcpyDeviceToHost, g->stream));
+        FL_CU(cudaMemcpyAsync(g->h_len.data(), g->d_len, g->nnz * 8, cudaMemcpyDeviceToHost, g->stream));
+    }
+    FL_CU(cudaStreamSynchronize(g->stream));
+    return FL_OK;
+}
+
+// Rows of the listed sites gathered into a compact CSR (list order).
+__global__ void k_row_degrees(uint32_t c, const uint32_t* __restrict__ ids,
+                              const uint32_t* __restrict__ row, uint32_t* __restrict__ deg) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < c) deg[i] = row[ids[i] + 1] - row[ids[i]];
+}
+__global__ void k_row_gather(uint32_t c, const uint32_t* __restrict__ ids,
+                             const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
+                             const double* __restrict__ len, const uint32_t* __restrict__ off,
+                             uint32_t* __restrict__ ocol, double* __restrict__ olen) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c) return;
+    uint32_t d = off[i];
+    for (uint32_t s = row[ids[i]], e = row[ids[i] + 1]; s < e; ++s, ++d) {
+        ocol[d] = col[s];
+        olen[d] = len[s];
+    }
+}
+
+// The lake heap's tied prefix for an outlet list (device ids; packed terrains one after
+// another, each replayed with its own heap), from the outlets' rows gathered on the
+// device.  *status: FL_OK, 1 for a NaN length, 2 when a zero-length edge reaches a site
+// that is not an outlet (then only the host heap over the whole graph can continue).
+int lake_prefix(fl_graph* g, const std::vector<uint32_t>& outlets, std::vector<uint32_t>& prefix,
+                int* status) {
+    prefix.clear();
+    *status = FL_OK;
+    const uint32_t c = (uint32_t)outlets.size();
+    if (c == 0) return FL_OK;
+    uint32_t *d_ids = nullptr, *d_deg = nullptr, *d_ocol = nullptr;
+    double* d_olen = nullptr;
+    std::vector<uint32_t> orow(c + 1ull), ocol;
+    std::vector<double> olen;
+    cudaError_t e = cudaMallocAsync((void**)&d_ids, c * 8ull, g->stream);
+    if (e == cudaSuccess) {
+        d_deg = d_ids + c;
+        e = cudaMemcpyAsync(d_ids, outlets.data(), c * 4ull, cudaMemcpyHostToDevice, g->stream);
+    }
+    if (e == cudaSuccess) {
+        k_row_degrees<<<blocks_for(c), kThreads, 0, g->stream>>>(c, d_ids, g->d_row, d_deg);
+        e = cudaMemcpyAsync(orow.data() + 1, d_deg, c * 4ull, cudaMemcpyDeviceToHost, g->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e == cudaSuccess) {
+        orow[0] = 0;
+        for (uint32_t i = 0; i < c; ++i) orow[i + 1] += orow[i];
+        ocol.resize(orow[c]);
+        olen.resize(orow[c]);
+        e = cudaMallocAsync((void**)&d_ocol, (orow[c] + 2ull) * 12ull, g->stream);
+    }
+    if (e == cudaSuccess) {
+        d_olen = (double*)(d_ocol + ((orow[c] + 1) & ~1u));   // 8-byte aligned after the columns
+        e = cudaMemcpyAsync(d_deg, orow.data(), c * 4ull, cudaMemcpyHostToDevice, g->stream);
+    }
+    if (e == cudaSuccess) {
+        k_row_gather<<<blocks_for(c), kThreads, 0, g->stream>>>(c, d_ids, g->d_row, g->d_col,
+                                                                g->d_len, d_deg, d_ocol, d_olen);
+        if (orow[c]) {
+            e = cudaMemcpyAsync(ocol.data(), d_ocol, orow[c] * 4ull, cudaMemcpyDeviceToHost, g->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(olen.data(), d_olen, orow[c] * 8ull, cudaMemcpyDeviceToHost, g->stream);
+        }
+    }
+    if (d_ocol) cudaFreeAsync(d_ocol, g->stream);
+    if (d_ids) cudaFreeAsync(d_ids, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) {
+        set_err("outlet rows", e);
+        return FL_ERR_CUDA;
+    }
+    std::vector<uint32_t> part;
+    size_t p0 = 0;
+    for (uint32_t t = 0; t < g->terrains; ++t) {
+        const uint32_t b = g->site_off[t + 1];
+        size_t p1 = p0;
+        while (p1 < c && outlets[p1] < b) ++p1;
+        const int r = fl::lake_rank_prefix_rows(g->n, outlets.data() + p0, (uint32_t)(p1 - p0),
+                                                orow.data() + p0, ocol.data(), olen.data(), part);
+        if (r != 0) {
+            *status = r;
+            return FL_OK;
+        }
+        prefix.insert(prefix.end(), part.begin(), part.end());
+        p0 = p1;
+    }
+    return FL_OK;
+}
+
 // Uploads the outlet list and table, computing (or reusing) the lake-heap rank.
 int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_rank) {
     uint32_t n = g->n;
@@ -752,35 +852,17 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
         // moves by its own pops), and lakes compare ranks within their terrain only.
         const auto t0 = std::chrono::steady_clock::now();
         std::vector<uint32_t> prefix;
-        if (g->terrains == 1) {
-            if (!fl::lake_rank_prefix(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
-                                      outlets.data(), (uint32_t)outlets.size(), prefix)) {
-                g_err = "NaN edge length in the lake traversal";
-                return FL_ERR_INVALID_ARGUMENT;
-            }
-        } else {
-            std::vector<uint32_t> lrow, lcol, lout, lpre;
-            size_t oi = 0;
-            for (uint32_t t = 0; t < g->terrains; ++t) {
-                const uint32_t a = g->site_off[t], b = g->site_off[t + 1], m = b - a;
-                const uint32_t s0 = g->h_row[a];
-                lrow.resize(m + 1);
-                for (uint32_t j = 0; j <= m; ++j) lrow[j] = g->h_row[a + j] - s0;
-                lcol.resize(g->h_row[b] - s0);
-                for (uint32_t s = s0; s < g->h_row[b]; ++s) lcol[s - s0] = g->h_col[s] - a;
-                lout.clear();
-                while (oi < outlets.size() && outlets[oi] < b) lout.push_back(outlets[oi++] - a);
-                if (!fl::lake_rank_prefix(m, lrow.data(), lcol.data(), g->h_len.data() + s0,
-                                          lout.data(), (uint32_t)lout.size(), lpre)) {
-                    g_err = "NaN edge length in the lake traversal";
-                    return FL_ERR_INVALID_ARGUMENT;
-                }
-                for (uint32_t v : lpre) prefix.push_back(a + v);
-            }
+        int pr = FL_OK;
+        FL_TRY(lake_prefix(g, outlets, prefix, &pr));
+        if (pr == 1) {
+            g_err = "NaN edge length in the lake traversal";
+            return FL_ERR_INVALID_ARGUMENT;
         }
         fl::GpuRankInfo info;
-        const fl::RankResult r = fl::gpu_lake_rank(g->stream, n, g->d_row, g->d_col, g->d_len,
-                                                   g->nnz, prefix, g->d_rank, g->d_sor, &info);
+        const fl::RankResult r =
+            pr != FL_OK ? fl::kRankFallback   // a zero-length edge: the host heap decides
+                        : fl::gpu_lake_rank(g->stream, n, g->d_row, g->d_col, g->d_len, g->nnz,
+                                            prefix, g->d_rank, g->d_sor, &info);
         if (r == fl::kRankError) {
             set_err("lake order on the GPU", info.error);
             return FL_ERR_CUDA;
@@ -798,6 +880,7 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
     if (need_rank && !g->rank_uploaded) {
         const auto t0 = std::chrono::steady_clock::now();
         if (!g->rank_valid || g->h_rank.size() != n) {
+            FL_TRY(ensure_host_csr(g));
             g->h_rank.resize(n);
             if (g->terrains == 1) {
                 if (!fl::lake_heap_rank(n, g->h_row.data(), g->h_col.data(), g->h_len.data(),
@@ -1189,19 +1272,11 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
                 return FL_ERR_INVALID_ARGUMENT;
             }
     }
-    uint64_t nnz = row_ptr[n];
+    const uint64_t nnz = row_ptr[n];
     if (row_ptr[0] != 0) { g_err = "row_ptr[0] != 0"; return FL_ERR_INVALID_ARGUMENT; }
-    for (uint32_t i = 0; i < n; ++i)
-        if (row_ptr[i + 1] < row_ptr[i]) { g_err = "row_ptr not monotone"; return FL_ERR_INVALID_ARGUMENT; }
-    for (uint64_t s = 0; s < nnz; ++s)
-        if (col[s] >= n || std::isnan(len[s])) { g_err = "column out of range or NaN length"; return FL_ERR_INVALID_ARGUMENT; }
+    if (nnz >= 0xffffffffull) { g_err = "more than 2^32 - 2 adjacency slots"; return FL_ERR_INVALID_ARGUMENT; }
+    // default outlets: in their terrain, not repeated (the rest is checked on the device)
     for (uint32_t t = 0; t < k_terr; ++t) {
-        for (uint32_t i = so[t]; i < so[t + 1]; ++i)
-            for (uint32_t s = row_ptr[i]; s < row_ptr[i + 1]; ++s)
-                if (col[s] < so[t] || col[s] >= so[t + 1]) {
-                    g_err = "an edge crosses two terrains";
-                    return FL_ERR_INVALID_ARGUMENT;
-                }
         std::vector<uint8_t> seen(so[t + 1] - so[t], 0);
         for (uint32_t i = dof[t]; i < dof[t + 1]; ++i) {
             const uint32_t o = default_outlets[i];
@@ -1223,25 +1298,7 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
     } track(&g->dev_bytes);
     g->site_off = so;
     g->def_off = dof;
-    g->perm.resize(n);
-    for (uint32_t t = 0; t < k_terr; ++t) {
-        const uint32_t a = so[t], m = so[t + 1] - so[t];
-        g->noise_n = std::max(g->noise_n, m);
-        if (xs && ys) {
-            std::vector<uint32_t> lp;
-            fl::hilbert_order(m, xs + a, ys + a, lp);
-            for (uint32_t j = 0; j < m; ++j) g->perm[a + j] = a + lp[j];
-        } else {
-            for (uint32_t j = 0; j < m; ++j) g->perm[a + j] = a + j;
-        }
-    }
-    g->inv.resize(n);
-    for (uint32_t j = 0; j < n; ++j) g->inv[g->perm[j]] = j;
-    fl::relabel_csr(n, row_ptr, col, len, g->perm, g->inv, g->h_row, g->h_col, g->h_len);
-    g->def_outlets.resize(n_default);
-    for (uint32_t i = 0; i < n_default; ++i) g->def_outlets[i] = g->inv[default_outlets[i]];
-    std::vector<double> parea(n);
-    for (uint32_t j = 0; j < n; ++j) parea[j] = area[g->perm[j]];
+    for (uint32_t t = 0; t < k_terr; ++t) g->noise_n = std::max(g->noise_n, so[t + 1] - so[t]);
     int rc = FL_OK;
     auto fail = [&](int r) { free_graph(g); return r; };
     cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
@@ -1255,43 +1312,33 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
         (rc = dalloc(&g->d_area, n)) ||
         (rc = dalloc(&g->d_perm, n)) || (rc = dalloc(&g->d_inv, n)) || (rc = alloc_workspace(g)))
         return fail(rc);
-    if (cudaMemcpy(g->d_row, g->h_row.data(), (n + 1) * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
-        (nnz && cudaMemcpy(g->d_col, g->h_col.data(), nnz * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) ||
-        (nnz && cudaMemcpy(g->d_len, g->h_len.data(), nnz * 8ull, cudaMemcpyHostToDevice) != cudaSuccess) ||
-        cudaMemcpy(g->d_area, parea.data(), n * 8ull, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g->d_perm, g->perm.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g->d_inv, g->inv.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) {
-        g_err = "graph upload failed";
-        return fail(FL_ERR_CUDA);
-    }
-    // the copies above ran on the default stream: let them land before the solver's
-    // stream reads the lengths
-    if (cudaStreamSynchronize(0) != cudaSuccess) {
-        g_err = "graph upload failed";
-        return fail(FL_ERR_CUDA);
+    if (k_terr > 1 &&
+        ((rc = dalloc(&g->d_noise_idx, n)) || (rc = dalloc(&g->d_tid, n)) ||
+         (rc = dalloc(&g->d_tchg, k_terr)) || (rc = dalloc(&g->d_titer, k_terr))))
+        return fail(rc);
+    // upload, check and relabel on the device
+    fl::GraphInput gi{n, nnz, row_ptr, col, len, area, (xs && ys) ? xs : nullptr,
+                      (xs && ys) ? ys : nullptr, k_terr, so.data()};
+    fl::GraphOutput go{g->d_row, g->d_col, g->d_len, g->d_area, g->d_perm, g->d_inv, g->d_tid,
+                       g->d_noise_idx};
+    std::string why;
+    rc = fl::build_device_graph(g->stream, gi, go, &why);
+    if (rc != FL_OK) {
+        g_err = why;
+        return fail(rc);
     }
     fl::launch_inv_len(g->stream, nnz, g->d_len, g->d_ilen);
-    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(g->stream) != cudaSuccess) {
-        g_err = "inverse edge lengths failed";
+    // the maps between caller and device order, kept on the host for the boundary
+    g->perm.resize(n);
+    g->inv.resize(n);
+    if (cudaMemcpyAsync(g->perm.data(), g->d_perm, n * 4ull, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
+        cudaMemcpyAsync(g->inv.data(), g->d_inv, n * 4ull, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
+        cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(g->stream) != cudaSuccess) {
+        g_err = "graph set-up on the device failed";
         return fail(FL_ERR_CUDA);
     }
-    if (k_terr > 1) {
-        // per device site: its sample of its terrain's noise stream, and its terrain
-        std::vector<uint32_t> nidx(n), tid(n);
-        for (uint32_t t = 0; t < k_terr; ++t)
-            for (uint32_t j = so[t]; j < so[t + 1]; ++j) {
-                nidx[j] = g->perm[j] - so[t];
-                tid[j] = t;
-            }
-        if ((rc = dalloc(&g->d_noise_idx, n)) || (rc = dalloc(&g->d_tid, n)) ||
-            (rc = dalloc(&g->d_tchg, k_terr)) || (rc = dalloc(&g->d_titer, k_terr)))
-            return fail(rc);
-        if (cudaMemcpy(g->d_noise_idx, nidx.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(g->d_tid, tid.data(), n * 4ull, cudaMemcpyHostToDevice) != cudaSuccess) {
-            g_err = "graph upload failed";
-            return fail(FL_ERR_CUDA);
-        }
-    }
+    g->def_outlets.resize(n_default);
+    for (uint32_t i = 0; i < n_default; ++i) g->def_outlets[i] = g->inv[default_outlets[i]];
     *out = g;
     return FL_OK;
 }
@@ -1443,6 +1490,7 @@ int fl_probe_tree_pass(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     FL_CU(cudaMemcpyAsync(g->d_next, nx.data(), n * 4ull, cudaMemcpyHostToDevice, g->stream));
     FL_TRY(upload_permuted(g, elev, g->d_elev));
     // receiver lengths as has_edge reports them (device order)
+    FL_TRY(ensure_host_csr(g));
     std::vector<double> rl(n);
     for (uint32_t j = 0; j < n; ++j) {
         rl[j] = 1.0;
@@ -1479,6 +1527,7 @@ int fl_probe_prim_rank(fl_graph* g, const uint32_t* outlets, uint32_t n_outlets,
     if (!g) return FL_ERR_MODEL_NOT_SET;
     std::vector<uint32_t> o = to_device_ids(g, outlets, n_outlets);
     std::vector<uint32_t> r(g->n);
+    FL_TRY(ensure_host_csr(g));
     if (!fl::lake_heap_rank(g->n, g->h_row.data(), g->h_col.data(), g->h_len.data(), o.data(),
                             n_outlets, r.data())) {
         g_err = "NaN edge length in the lake traversal";
@@ -1573,16 +1622,24 @@ int fl_probe_lake_rank_gpu(fl_graph* g, const uint32_t* outlets, uint32_t n_outl
     for (uint32_t i = 0; i < n_outlets; ++i)
         if (outlets[i] >= n) return FL_ERR_INVALID_ARGUMENT;
     std::vector<uint32_t> o = to_device_ids(g, outlets, n_outlets), prefix;
-    if (!fl::lake_rank_prefix(n, g->h_row.data(), g->h_col.data(), g->h_len.data(), o.data(),
-                              n_outlets, prefix)) {
+    int pr = FL_OK;
+    if (g->terrains > 1) {                     // the prefix replays terrain after terrain
+        g_err = "fl_probe_lake_rank_gpu takes a single-terrain model";
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    FL_TRY(lake_prefix(g, o, prefix, &pr));
+    if (pr == 1) {
         g_err = "NaN edge length in the lake traversal";
         return FL_ERR_INVALID_ARGUMENT;
     }
     // into the solver's rank arrays: the next lake pass recomputes its own order
     g->rank_valid = g->rank_uploaded = false;
     fl::GpuRankInfo info;
-    const fl::RankResult r = fl::gpu_lake_rank(g->stream, n, g->d_row, g->d_col, g->d_len, g->nnz,
-                                               prefix, g->d_rank, g->d_sor, &info);
+    if (pr == 2) info.fallback_reason = "a zero-length edge reaches a site at key 0.0";
+    const fl::RankResult r =
+        pr == 2 ? fl::kRankFallback
+                : fl::gpu_lake_rank(g->stream, n, g->d_row, g->d_col, g->d_len, g->nnz, prefix,
+                                    g->d_rank, g->d_sor, &info);
     if (r == fl::kRankError) {
         set_err("lake order on the GPU", info.error);
         return FL_ERR_CUDA;
