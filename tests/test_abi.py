@@ -72,24 +72,35 @@ def test_parameter_defaults_and_setters():
     assert np.isnan(arr.max_slope[0]) and arr.max_slope[1] == 0.3
 
 
-def test_batch_create_rejects_edges_across_terrains(fl_lib):
-    """Packed terrains must not share an edge (checked before any device work)."""
-    import ctypes
+def _two_joined_terrains():
     import numpy as np
-    from fastlem_gb300._lib import FL_ERR_INVALID_ARGUMENT, ptr
     # two 2-site terrains; site 1 (terrain 0) is joined to site 2 (terrain 1)
-    site_off = np.array([0, 2, 4], np.uint32)
-    row_ptr = np.array([0, 1, 3, 5, 6], np.uint32)
-    col = np.array([1, 0, 2, 1, 3, 2], np.uint32)
-    length = np.ones(6)
-    area = np.ones(4)
-    def_off = np.array([0, 1, 2], np.uint32)
-    defs = np.array([0, 3], np.uint32)
+    return (np.array([0, 2, 4], np.uint32), np.array([0, 1, 3, 5, 6], np.uint32),
+            np.array([1, 0, 2, 1, 3, 2], np.uint32), np.ones(6), np.ones(4),
+            np.array([0, 1, 2], np.uint32), np.array([0, 3], np.uint32))
+
+
+@pytest.mark.gpu
+def test_batch_create_rejects_edges_across_terrains(fl_lib):
+    """Packed terrains must not share an edge (checked on the device with the rest of
+    the graph, before the model is returned)."""
+    import ctypes
+    from fastlem_gb300._lib import FL_ERR_INVALID_ARGUMENT, ptr
+    site_off, row_ptr, col, length, area, def_off, defs = _two_joined_terrains()
     h = ctypes.c_void_p()
     rc = fl_lib.fl_batch_create(2, ptr(site_off), ptr(row_ptr), ptr(col), ptr(length), ptr(area),
                                 ptr(def_off), ptr(defs), None, None, ctypes.byref(h))
     assert rc == FL_ERR_INVALID_ARGUMENT
     assert b"cross" in fl_lib.fl_last_error()
+
+
+def test_batch_create_rejects_bad_offsets(fl_lib):
+    """Terrain offsets that do not cover the sites (checked before any device work)."""
+    import ctypes
+    import numpy as np
+    from fastlem_gb300._lib import FL_ERR_INVALID_ARGUMENT, ptr
+    site_off, row_ptr, col, length, area, def_off, defs = _two_joined_terrains()
+    h = ctypes.c_void_p()
     # offsets that do not cover the sites
     rc = fl_lib.fl_batch_create(2, ptr(np.array([0, 2, 3], np.uint32)), ptr(row_ptr), ptr(col),
                                 ptr(length), ptr(area), ptr(def_off), ptr(defs), None, None,
