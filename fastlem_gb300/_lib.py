@@ -106,7 +106,8 @@ def lib():
     L.fl_get_tuning.argtypes = [ctypes.c_char_p]
     L.fl_get_tuning.restype = ctypes.c_int64
     L.fl_graph_rank_info.argtypes = [vp, P(c_dbl), P(c_int)]
-    L.fl_schedule_entry.argtypes = [c_u32, P(c_u32), P(c_int), P(c_int), P(c_u32), P(c_u32)]
+    L.fl_schedule_entry.argtypes = [c_u32, P(c_u32), P(c_int), P(c_int), P(c_u32), P(c_u32),
+                                    P(c_int)]
     L.fl_probe_lake_rank_gpu.argtypes = [vp, vp, c_u32, vp, P(c_int)]
     L.fl_num_kernel_classes.restype = c_u32
     L.fl_graph_kernel_stats.argtypes = [vp, c_u32, P(ctypes.c_char_p), P(c_u64), P(c_dbl), P(c_dbl)]
@@ -199,7 +200,7 @@ def kernel_stats(handle):
     return out
 
 
-TUNING = ("low_ilp", "walk_per_sm", "gpu_rank", "kahn_min_width")
+TUNING = ("low_ilp", "walk_per_sm", "sized_grids", "gpu_rank", "kahn_min_width")
 
 
 def set_tuning(**kw):
@@ -215,11 +216,11 @@ def set_tuning(**kw):
 
 def schedule():
     """The library's compiled-in schedule: [(max_sites, packed, low_ilp, walk_per_sm,
-    kahn_min_width)]."""
+    kahn_min_width, sized_grids)]."""
     out = []
     i = 0
     while True:
-        v = [c_u32(), c_int(), c_int(), c_u32(), c_u32()]
+        v = [c_u32(), c_int(), c_int(), c_u32(), c_u32(), c_int()]
         if lib().fl_schedule_entry(i, *[ctypes.byref(x) for x in v]) != FL_OK:
             return out
         out.append(tuple(int(x.value) for x in v))

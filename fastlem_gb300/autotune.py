@@ -9,7 +9,8 @@ size -- it times generate() with set_max_iteration(8) (device time of the iterat
 loop, after two warm-up solves) while varying, one knob at a time:
   kahn_min_width  where the Kahn rounds stop and the skeleton chain walks take over (the
                   round-versus-chain switch): the default rule n / 512 clamped to
-                  [8192, 65536], times 1/4, 1/2, 2 and 4;
+                  [8192, 65536], times 1/16, 1/8, 1/4, 1/2 and 2;
+  sized_grids     cooperative grids cut to the model's size, or the whole GPU;
   low_ilp         sites in flight per thread in the top-down Kahn rounds (1, 2, 4);
   walk_per_sm     chain walker blocks per SM (all that fit, 4, 2).
 Each knob keeps the best value found before the next is tried.  The results go to a
@@ -68,34 +69,42 @@ def sweep(timer, n, log):
     """Coordinate sweep of the three knobs for one class; returns (default, best, trials)."""
     trials = []
 
-    def run(width, ilp, walk):
-        old = _lib.set_tuning(kahn_min_width=width, low_ilp=ilp, walk_per_sm=walk)
+    def run(width, ilp, walk, sized):
+        old = _lib.set_tuning(kahn_min_width=width, low_ilp=ilp, walk_per_sm=walk,
+                              sized_grids=sized)
         try:
             ms = timer()
         finally:
             _lib.set_tuning(**old)
-        t = {"kahn_min_width": width, "low_ilp": ilp, "walk_per_sm": walk, "ms_per_iteration": ms}
+        t = {"kahn_min_width": width, "low_ilp": ilp, "walk_per_sm": walk, "sized_grids": sized,
+             "ms_per_iteration": ms}
         trials.append(t)
-        log(f"  width {width:>7} ilp {ilp} walk/SM {walk}: {ms:.3f} ms/iteration")
+        log(f"  width {width:>7} ilp {ilp} walk/SM {walk} sized {sized}: {ms:.3f} ms/iteration")
         return ms
 
     rule = _rule(n)
-    default = {"kahn_min_width": 0, "low_ilp": 4, "walk_per_sm": 0}
-    default["ms_per_iteration"] = run(0, 4, 0)
+    default = {"kahn_min_width": 0, "low_ilp": 4, "walk_per_sm": 0, "sized_grids": 0}
+    default["ms_per_iteration"] = run(0, 4, 0, 0)
     best = dict(default)
-    for f in (0.25, 0.5, 2.0, 4.0):
-        width = int(max(256, min(1 << 20, rule * f)))
-        ms = run(width, best["low_ilp"], best["walk_per_sm"])
+
+    def knobs(**kw):
+        d = {k: best[k] for k in ("kahn_min_width", "low_ilp", "walk_per_sm", "sized_grids")}
+        d.update(kw)
+        return d
+
+    def tryit(**kw):
+        k = knobs(**kw)
+        ms = run(k["kahn_min_width"], k["low_ilp"], k["walk_per_sm"], k["sized_grids"])
         if ms < best["ms_per_iteration"]:
-            best.update(kahn_min_width=width, ms_per_iteration=ms)
+            best.update(k, ms_per_iteration=ms)
+
+    for f in (0.0625, 0.125, 0.25, 0.5, 2.0):
+        tryit(kahn_min_width=int(max(256, min(1 << 20, rule * f))))
+    tryit(sized_grids=1)
     for ilp in (1, 2):
-        ms = run(best["kahn_min_width"], ilp, best["walk_per_sm"])
-        if ms < best["ms_per_iteration"]:
-            best.update(low_ilp=ilp, ms_per_iteration=ms)
+        tryit(low_ilp=ilp)
     for walk in (4, 2):
-        ms = run(best["kahn_min_width"], best["low_ilp"], walk)
-        if ms < best["ms_per_iteration"]:
-            best.update(walk_per_sm=walk, ms_per_iteration=ms)
+        tryit(walk_per_sm=walk)
     return default, best, trials
 
 
@@ -134,7 +143,8 @@ def main():
     for c in classes:
         s = c["best"]
         log(f"        {{{c['max_sites']:#x}u, {'true' if c['packed'] else 'false'}, "
-            f"{{{s['low_ilp']}, {s['walk_per_sm']}, {s['kahn_min_width']}}}}},")
+            f"{{{s['low_ilp']}, {s['walk_per_sm']}, {s['kahn_min_width']}, "
+            f"{'true' if s['sized_grids'] else 'false'}}}}},")
 
 
 def _device_name():

@@ -1525,13 +1525,16 @@ uint32_t walk_grid(uint32_t per_sm) {
 cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uint32_t nnz) {
     const uint32_t n = a.n;
     const unsigned nb = (n + kThreads - 1) / kThreads;
-    const unsigned g_kahn = coop_grid((const void*)k_kahn, kThreads, 8);
-    const unsigned g_rank = coop_grid((const void*)k_s_rank, kRoundBlock, 2);
+    const bool sz = a.sized_grids;
+    const unsigned g_kahn = sized_grid(sz, coop_grid((const void*)k_kahn, kThreads, 8), n, kThreads * 8);
+    const unsigned g_rank = sized_grid(sz, coop_grid((const void*)k_s_rank, kRoundBlock, 2), n / 8,
+                                       kRoundBlock * 4);
     // ordered compactions: one block range each, two blocks per SM
     const unsigned g_compact = coop_grid((const void*)k_collect_leaves, kRoundBlock, 2);
     // persistent chain walkers: every warp resident (they wait on one another)
-    const unsigned g_chain = a.walk_grid;
-    const unsigned g_tree = coop_grid((const void*)k_s_chain_tree, kThreads, 4);
+    const unsigned g_chain = sized_grid(sz, a.walk_grid, n, 4096, 16);
+    const unsigned g_tree = sized_grid(sz, coop_grid((const void*)k_s_chain_tree, kThreads, 4), n / 16,
+                                       kThreads * 4);
     const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
     TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.rec_t, a.elev, a.flags, a.tid, a.tchg};
@@ -1581,7 +1584,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
                     (const uint32_t*)a.layout, (const uint32_t*)a.coff, (const uint32_t*)a.sid,
                     (const uint32_t*)a.kslot, (const uint32_t*)a.slot_chain, a.cpar1, a.cdep,
                     a.cpar1 + a.kahn_min_width, a.cdep1, a.cqp, a.cpar, a.chist, a.corder,
-                    a.corder_up, a.walk_grid * kWalkWarps, a.meta, a.flags);
+                    a.corder_up, g_chain * kWalkWarps, a.meta, a.flags);
     if (e != cudaSuccess) return e;
     k_s_prepare<<<gs, kThreads, 0, st>>>(n, a.row, a.col, a.next, a.hgt, a.area, a.A, a.layout,
                                          a.slot_chain, a.coff, a.clen, a.cbot, a.rec, a.info,
@@ -1655,7 +1658,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
                               : K == 2 ? (const void*)k_low_top_down<false, 2>
                                        : (const void*)k_low_top_down<false, 1>);
         const unsigned blk = (unsigned)low_block(K);
-        e = coop_launch_ptr(kern, coop_grid(kern, blk, 2048 / blk), blk, st, td,
+        e = coop_launch_ptr(kern, sized_grid(sz, coop_grid(kern, blk, 2048 / blk), n, blk * 16ull), blk, st, td,
                             (const uint32_t*)a.order, (const uint32_t*)a.roff,
                             a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta, a.all_records);
     }

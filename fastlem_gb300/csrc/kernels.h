@@ -33,6 +33,7 @@ struct Shape {
     uint32_t walk_per_sm;     // chain walker blocks per SM; 0: as many as fit
     uint32_t kahn_min_width;  // Kahn rounds stop below this frontier width; 0: n / 512
                               // clamped to [8192, 65536]
+    bool sized_grids;         // cooperative grids scaled to the model (else the whole GPU)
 };
 // The schedule: per size class (models of up to max_sites sites; packed batches apart)
 // the shapes the schedule sweep chose on GB300 (fastlem_gb300/schedule.json).
@@ -49,6 +50,7 @@ struct Tuning {
     int low_ilp = -1;
     int walk_per_sm = -1;
     int64_t kahn_min_width = -1;
+    int sized_grids = -1;
     bool gpu_rank = true;
 };
 Tuning& tuning();
@@ -60,6 +62,16 @@ Shape shape_for(uint32_t n, bool packed);
 // warps) for the current tuning.
 uint32_t walk_capacity();
 uint32_t walk_grid(uint32_t per_sm);
+// A cooperative grid of `full` co-resident blocks cut to `units` of work at
+// `per_block` each (at least min_blocks) when sized grids are on: a small model then
+// leaves most of the GPU to the solves of other streams.
+inline unsigned sized_grid(bool sized, unsigned full, uint64_t units, uint64_t per_block,
+                           unsigned min_blocks = 4) {
+    if (!sized) return full;
+    const uint64_t want = (units + per_block - 1) / per_block;
+    const uint64_t b = want < min_blocks ? min_blocks : want;
+    return (unsigned)(b < full ? b : full);
+}
 
 // Device-side bookkeeping words of one basin pass (uint32 slots of BasinArgs::meta).
 enum Meta {
@@ -180,6 +192,7 @@ struct BasinArgs {
     uint32_t* corder_up;    // chains by height, lowest first: the bottom-up claim order
     uint32_t walk_grid;     // blocks of the persistent chain walkers (all co-resident)
     int low_ilp;            // top-down Kahn rounds: sites in flight per thread
+    bool sized_grids;       // cooperative grids scaled to n (else the whole GPU)
     double* el;             // skeleton elevations in layout order (slope limits only)
     uint32_t* cbas;         // per chain: basin outlet, its response time and elevation
     double* cto;

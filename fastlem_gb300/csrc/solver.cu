@@ -327,6 +327,7 @@ Tuning& tuning() {
         d.walk_per_sm = (int)env("FL_WALK_PER_SM", 0, 64, -1);
         d.kahn_min_width = env("FL_KAHN_MIN_WIDTH", 256, 1l << 24, -1);
         d.gpu_rank = env("FL_GPU_RANK", 0, 1, 1) != 0;
+        d.sized_grids = (int)env("FL_SIZED_GRIDS", 0, 1, -1);
         return d;
     }();
     return t;
@@ -337,18 +338,18 @@ Tuning& tuning() {
 const std::vector<ScheduleEntry>& schedule() {
     static const std::vector<ScheduleEntry> s = {
         // max_sites, packed, {low_ilp, walk_per_sm, kahn_min_width}
-        {0x20000u, false, {4, 4, 2048}},
-        {0x80000u, false, {4, 4, 2048}},
-        {0x200000u, false, {4, 0, 4096}},
-        {0x7d0000u, false, {4, 0, 4096}},
-        {0xffffffffu, false, {4, 4, 0}},
-        {0xffffffffu, true, {2, 0, 0}},
+        {0x20000u, false, {4, 4, 2048, false}},
+        {0x80000u, false, {4, 4, 2048, false}},
+        {0x200000u, false, {4, 0, 4096, false}},
+        {0x7d0000u, false, {4, 0, 4096, false}},
+        {0xffffffffu, false, {4, 4, 0, false}},
+        {0xffffffffu, true, {2, 0, 0, false}},
     };
     return s;
 }
 
 Shape shape_for(uint32_t n, bool packed) {
-    Shape sh{4, 0, 0};
+    Shape sh{4, 0, 0, false};
     for (const ScheduleEntry& e : schedule())
         if (e.packed == packed && n <= e.max_sites) {
             sh = e.shape;
@@ -358,6 +359,7 @@ Shape shape_for(uint32_t n, bool packed) {
     if (t.low_ilp > 0) sh.low_ilp = t.low_ilp;
     if (t.walk_per_sm >= 0) sh.walk_per_sm = (uint32_t)t.walk_per_sm;
     if (t.kahn_min_width >= 0) sh.kahn_min_width = (uint32_t)t.kahn_min_width;
+    if (t.sized_grids >= 0) sh.sized_grids = t.sized_grids != 0;
     return sh;
 }
 }  // namespace fl
@@ -941,7 +943,8 @@ int enqueue_receivers(fl_graph* g) {
 // gate, only if *gate is set when the kernel runs.
 int enqueue_labels(fl_graph* g, const int* gate) {
     uint32_t n = g->n;
-    static const unsigned grid = coop_blocks((const void*)k_labels, 1024, 2);
+    static const unsigned full = coop_blocks((const void*)k_labels, 1024, 2);
+    const unsigned grid = fl::sized_grid(fl::shape_for(n, g->terrains > 1).sized_grids, full, n, 1024 * 8);
     const int* gt = gate;
     void* argv[] = {(void*)&n, (void*)&g->d_next, (void*)&g->d_lab, (void*)&g->d_lab2,
                     (void*)&gt, (void*)&g->d_flags};
@@ -1065,6 +1068,7 @@ int enqueue_basin_pass(fl_graph* g, bool all_records = false) {
     const fl::Shape sh = fl::shape_for(g->n, g->terrains > 1);
     a.walk_grid = fl::walk_grid(sh.walk_per_sm);
     a.low_ilp = sh.low_ilp;
+    a.sized_grids = sh.sized_grids;
     a.rec = g->d_rec;
     a.info = g->d_info;
     a.needl = g->d_needl;
@@ -1572,6 +1576,8 @@ int fl_set_tuning(const char* name, int64_t value) {
         t.low_ilp = (int)value;
     } else if (k == "walk_per_sm" && value >= -1 && value <= 64) {
         t.walk_per_sm = (int)value;
+    } else if (k == "sized_grids" && value >= -1 && value <= 1) {
+        t.sized_grids = (int)value;
     } else if (k == "gpu_rank" && (value == 0 || value == 1)) {
         t.gpu_rank = value != 0;
     } else if (k == "kahn_min_width" &&
@@ -1591,11 +1597,12 @@ int64_t fl_get_tuning(const char* name) {
     if (k == "walk_per_sm") return t.walk_per_sm;
     if (k == "kahn_min_width") return t.kahn_min_width;
     if (k == "gpu_rank") return t.gpu_rank ? 1 : 0;
+    if (k == "sized_grids") return t.sized_grids;
     return -2;
 }
 
 int fl_schedule_entry(uint32_t i, uint32_t* max_sites, int* packed, int* low_ilp,
-                      uint32_t* walk_per_sm, uint32_t* kahn_min_width) {
+                      uint32_t* walk_per_sm, uint32_t* kahn_min_width, int* sized_grids) {
     const auto& s = fl::schedule();
     if (i >= s.size()) return FL_ERR_INVALID_ARGUMENT;
     if (max_sites) *max_sites = s[i].max_sites;
@@ -1603,6 +1610,7 @@ int fl_schedule_entry(uint32_t i, uint32_t* max_sites, int* packed, int* low_ilp
     if (low_ilp) *low_ilp = s[i].shape.low_ilp;
     if (walk_per_sm) *walk_per_sm = s[i].shape.walk_per_sm;
     if (kahn_min_width) *kahn_min_width = s[i].shape.kahn_min_width;
+    if (sized_grids) *sized_grids = s[i].shape.sized_grids ? 1 : 0;
     return FL_OK;
 }
 

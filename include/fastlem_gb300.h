@@ -210,16 +210,18 @@ uint64_t fl_graph_host_syncs(const fl_graph* g);
  *   "kahn_min_width" Kahn rounds stop below this frontier width (where the chain walks
  *                    take over), 256 .. 2^24, or 0 for n / 512 clamped to [8192, 65536];
  *                    read when a model is created
+ *   "sized_grids"    1: cooperative grids cut to the model's size (small models leave the
+ *                    rest of the GPU to other streams' solves), 0: whole-GPU grids
  *   "gpu_rank"       1: the lake heap's order computed on the GPU where lengths decide it
  *                    (the host heap otherwise), 0: always the host heap
- * Change them only while no solve runs.  FL_LOW_ILP, FL_WALK_PER_SM, FL_KAHN_MIN_WIDTH and
- * FL_GPU_RANK in the environment set them at load. */
+ * Change them only while no solve runs.  FL_LOW_ILP, FL_WALK_PER_SM, FL_KAHN_MIN_WIDTH,
+ * FL_SIZED_GRIDS and FL_GPU_RANK in the environment set them at load. */
 int fl_set_tuning(const char* name, int64_t value);
 int64_t fl_get_tuning(const char* name);   /* -2 for an unknown name */
 /* Schedule entry i (FL_ERR_INVALID_ARGUMENT past the end): models of up to max_sites
  * sites (packed batches when packed is 1) use these shapes; 0 width = the n / 512 rule. */
 int fl_schedule_entry(uint32_t i, uint32_t* max_sites, int* packed, int* low_ilp,
-                      uint32_t* walk_per_sm, uint32_t* kahn_min_width);
+                      uint32_t* walk_per_sm, uint32_t* kahn_min_width, int* sized_grids);
 
 /* Where and how long the model's last lake-order computation ran: *on_gpu 1 (GPU), 0
  * (host heap) or -1 (none yet); *ms its host wall time. */

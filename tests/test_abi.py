@@ -203,5 +203,5 @@ def test_compiled_schedule_is_the_committed_one(fl_lib):
     with open(path) as f:
         classes = json.load(f)["classes"]
     want = [(c["max_sites"], int(c["packed"]), c["best"]["low_ilp"], c["best"]["walk_per_sm"],
-             c["best"]["kahn_min_width"]) for c in classes]
+             c["best"]["kahn_min_width"], int(c["best"].get("sized_grids", 0))) for c in classes]
     assert _lib.schedule() == want

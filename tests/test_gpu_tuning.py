@@ -1,7 +1,7 @@
 """Every launch shape the schedule can choose gives the same bits.
 
 The top-down Kahn rounds (1, 2 or 4 sites in flight per thread), the number of chain
-walkers per SM and the Kahn stop width (where the chain walks take over) only change
+walkers per SM, whole-GPU or model-sized cooperative grids and the Kahn stop width (where the chain walks take over) only change
 how the exact recurrences are scheduled, never their evaluation order, so generate()
 must return the oracle's elevations and iteration count under each of them."""
 import numpy as np
@@ -36,10 +36,11 @@ def _check(cases):
         w.model.release()
 
 
+@pytest.mark.parametrize("sized_grids", [0, 1])
 @pytest.mark.parametrize("walk_per_sm", [0, 2])
 @pytest.mark.parametrize("low_ilp", [1, 2, 4])
-def test_launch_shapes_give_the_oracle_bits(cases, walk_per_sm, low_ilp):
-    old = _lib.set_tuning(low_ilp=low_ilp, walk_per_sm=walk_per_sm)
+def test_launch_shapes_give_the_oracle_bits(cases, walk_per_sm, low_ilp, sized_grids):
+    old = _lib.set_tuning(low_ilp=low_ilp, walk_per_sm=walk_per_sm, sized_grids=sized_grids)
     try:
         _check(cases)
     finally:
