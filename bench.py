@@ -670,6 +670,10 @@ def bench_served(args, d, emit=True):
         "identical_to_plain": identical,
         "cpu_baseline": cpu,
         "server": stats,
+        # mean requests in service over the span (solve time of all requests / span)
+        "mean_in_service": float(sum(info["solve_ms"] for _, info in served) / (span * 1000)),
+        "queue_ms": {"p50": float(np.percentile([i["queue_ms"] for _, i in served], 50)),
+                     "max": float(max(i["queue_ms"] for _, i in served))},
         "clocks": clocks.summary(),
     }
     if emit:

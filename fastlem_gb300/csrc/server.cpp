@@ -183,6 +183,8 @@ void worker(fl_server* s) {
                                  m.coords ? m.xs.data() : nullptr,
                                  m.coords ? m.ys.data() : nullptr, &inst);
             if (rc != FL_OK) err = fl_last_error();
+            // concurrent solves: small models take only part of the GPU
+            if (rc == FL_OK) fl_graph_set_sized_grids(inst, 1);
         }
         uint64_t real = inst ? fl_graph_device_bytes(inst) : 0;
         if (rc == FL_OK) {

@@ -338,12 +338,12 @@ Tuning& tuning() {
 const std::vector<ScheduleEntry>& schedule() {
     static const std::vector<ScheduleEntry> s = {
         // max_sites, packed, {low_ilp, walk_per_sm, kahn_min_width}
-        {0x20000u, false, {4, 4, 2048, false}},
-        {0x80000u, false, {4, 4, 2048, false}},
-        {0x200000u, false, {4, 0, 4096, false}},
-        {0x7d0000u, false, {4, 0, 4096, false}},
-        {0xffffffffu, false, {4, 4, 0, false}},
-        {0xffffffffu, true, {2, 0, 0, false}},
+        {0x20000u, false, {4, 2, 512, false}},
+        {0x80000u, false, {4, 0, 1024, true}},
+        {0x200000u, false, {4, 0, 2048, true}},
+        {0x7d0000u, false, {4, 0, 4096, true}},
+        {0xffffffffu, false, {4, 4, 0, true}},
+        {0xffffffffu, true, {2, 0, 0, true}},
     };
     return s;
 }
@@ -388,6 +388,7 @@ struct fl_graph {
     bool rank_uploaded = false;
     std::vector<uint32_t> h_rank;        // host-computed rank (empty when computed on the GPU)
     int rank_gpu = -1;                   // where the last rank was computed: 1 GPU, 0 host
+    int sized_grids = -1;                // model-sized cooperative grids: -1 the schedule's
     double rank_ms = 0.0;                // its host wall time
     // device order: perm[device index] = caller index, inv the reverse
     std::vector<uint32_t> perm, inv;
@@ -944,7 +945,9 @@ int enqueue_receivers(fl_graph* g) {
 int enqueue_labels(fl_graph* g, const int* gate) {
     uint32_t n = g->n;
     static const unsigned full = coop_blocks((const void*)k_labels, 1024, 2);
-    const unsigned grid = fl::sized_grid(fl::shape_for(n, g->terrains > 1).sized_grids, full, n, 1024 * 8);
+    const bool sized = g->sized_grids >= 0 ? g->sized_grids != 0
+                                           : fl::shape_for(n, g->terrains > 1).sized_grids;
+    const unsigned grid = fl::sized_grid(sized, full, n, 1024 * 8);
     const int* gt = gate;
     void* argv[] = {(void*)&n, (void*)&g->d_next, (void*)&g->d_lab, (void*)&g->d_lab2,
                     (void*)&gt, (void*)&g->d_flags};
@@ -1068,7 +1071,7 @@ int enqueue_basin_pass(fl_graph* g, bool all_records = false) {
     const fl::Shape sh = fl::shape_for(g->n, g->terrains > 1);
     a.walk_grid = fl::walk_grid(sh.walk_per_sm);
     a.low_ilp = sh.low_ilp;
-    a.sized_grids = sh.sized_grids;
+    a.sized_grids = g->sized_grids >= 0 ? g->sized_grids != 0 : sh.sized_grids;
     a.rec = g->d_rec;
     a.info = g->d_info;
     a.needl = g->d_needl;
@@ -1567,6 +1570,13 @@ int fl_graph_set_timing(fl_graph* g, int enable) {
 }
 
 uint64_t fl_graph_host_syncs(const fl_graph* g) { return g ? g->host_syncs : 0; }
+
+int fl_graph_set_sized_grids(fl_graph* g, int sized) {
+    if (!g) return FL_ERR_MODEL_NOT_SET;
+    if (sized < -1 || sized > 1) return FL_ERR_INVALID_ARGUMENT;
+    g->sized_grids = sized;
+    return FL_OK;
+}
 
 int fl_set_tuning(const char* name, int64_t value) {
     g_err.clear();

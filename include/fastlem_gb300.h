@@ -218,6 +218,10 @@ uint64_t fl_graph_host_syncs(const fl_graph* g);
  * FL_SIZED_GRIDS and FL_GPU_RANK in the environment set them at load. */
 int fl_set_tuning(const char* name, int64_t value);
 int64_t fl_get_tuning(const char* name);   /* -2 for an unknown name */
+/* This model's cooperative grids: 1 cut to its size, 0 the whole GPU, -1 as the
+ * schedule says.  A serving loop that runs several solves at once sets 1 on its
+ * instances so that small solves leave room for the others. */
+int fl_graph_set_sized_grids(fl_graph* g, int sized);
 /* Schedule entry i (FL_ERR_INVALID_ARGUMENT past the end): models of up to max_sites
  * sites (packed batches when packed is 1) use these shapes; 0 width = the n / 512 rule. */
 int fl_schedule_entry(uint32_t i, uint32_t* max_sites, int* packed, int* low_ilp,

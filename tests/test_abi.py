@@ -116,7 +116,7 @@ def test_server_host_checks(fl_lib):
                                     FL_ERR_OUT_OF_MEMORY, ptr)
     s = ctypes.c_void_p()
     assert fl_lib.fl_server_create(0, 2, ctypes.byref(s)) == FL_ERR_INVALID_ARGUMENT
-    assert fl_lib.fl_server_create(1 << 16, 1, ctypes.byref(s)) == 0
+    assert fl_lib.fl_server_create(1 << 14, 1, ctypes.byref(s)) == 0
     try:
         row_ptr = np.array([0, 1, 2], np.uint32)
         col = np.array([1, 0], np.uint32)
@@ -137,7 +137,7 @@ def test_server_host_checks(fl_lib):
         out = np.empty(2)
         t = ctypes.c_uint64()
         outl = np.zeros(2, np.uint8)
-        # unknown model, then a model whose instance can never fit a 64 KiB budget
+        # unknown model, then a model whose instance can never fit a 16 KiB budget
         assert fl_lib.fl_server_submit(s, 7, ptr(z), ptr(o), ptr(o), ptr(outl), None, -1,
                                        ptr(out), ctypes.byref(t)) == FL_ERR_MODEL_NOT_SET
         assert fl_lib.fl_server_submit(s, mid.value, ptr(z), ptr(o), ptr(o), ptr(outl), None, -1,
