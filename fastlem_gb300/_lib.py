@@ -30,7 +30,8 @@ EXPORTS = [
     "fl_graph_num_sites", "fl_graph_num_slots", "fl_last_error", "fl_select_device",
     "fl_graph_set_timing", "fl_graph_reset_stats", "fl_graph_host_syncs", "fl_set_tuning",
     "fl_get_tuning", "fl_graph_rank_info", "fl_probe_lake_rank_gpu",
-    "fl_schedule_entry", "fl_graph_set_sized_grids", "fl_num_kernel_classes",
+    "fl_schedule_entry", "fl_graph_set_sized_grids", "fl_batch_create_parts",
+    "fl_batch_generate_parts", "fl_server_set_packing", "fl_num_kernel_classes",
     "fl_graph_kernel_stats",
     "fl_graph_basin_stats", "fl_graph_round_trace", "fl_basin_labels_noalloc",
     "fl_batch_create", "fl_graph_num_terrains", "fl_batch_generate", "fl_graph_device_bytes",

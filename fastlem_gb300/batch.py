@@ -33,35 +33,26 @@ class TerrainBatch:
         return len(self.models)
 
     def handle(self):
+        """The packed device graph, built from every model's own arrays (no
+        concatenated host copy: fl_batch_create_parts)."""
         if self._handle is not None:
             return self._handle
-        rows, cols, lens, areas, xs, ys, defs = [], [], [], [], [], [], []
-        slot = 0
-        def_off = np.zeros(len(self.models) + 1, np.uint32)
-        for t, m in enumerate(self.models):
-            base = int(self.site_off[t])
-            rows.append(m.row_ptr[:-1].astype(np.uint64) + slot)
-            cols.append(m.col.astype(np.uint64) + base)
-            slot += int(m.row_ptr[-1])
-            lens.append(m.length)
-            areas.append(m.area)
-            xs.append(m.xs)
-            ys.append(m.ys)
-            defs.append(m.default_outlets.astype(np.uint64) + base)
-            def_off[t + 1] = def_off[t] + len(m.default_outlets)
-        if slot >= 0xFFFFFFFF:
+        k = len(self.models)
+        if sum(int(m.row_ptr[-1]) for m in self.models) >= 0xFFFFFFFF:
             raise ValueError("a batch holds fewer than 2^32 - 1 adjacency slots")
-        row_ptr = np.concatenate(rows + [np.array([slot], np.uint64)]).astype(np.uint32)
-        col = np.concatenate(cols).astype(np.uint32)
-        length = np.ascontiguousarray(np.concatenate(lens), np.float64)
-        area = np.ascontiguousarray(np.concatenate(areas), np.float64)
-        x = np.ascontiguousarray(np.concatenate(xs), np.float64)
-        y = np.ascontiguousarray(np.concatenate(ys), np.float64)
-        d = np.concatenate(defs).astype(np.uint32)
+        arr = lambda ctype, xs: (ctype * k)(*[x.ctypes.data_as(ctype) for x in xs])
+        u32p, f64p = ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_double)
+        ms = self.models
+        sites = np.array([m.num() for m in ms], np.uint32)
+        ndef = np.array([len(m.default_outlets) for m in ms], np.uint32)
+        have_xy = all(m.xs is not None and m.ys is not None for m in ms)
         h = ctypes.c_void_p()
-        check(lib().fl_batch_create(len(self.models), ptr(self.site_off), ptr(row_ptr), ptr(col),
-                                    ptr(length), ptr(area), ptr(def_off), ptr(d), ptr(x), ptr(y),
-                                    ctypes.byref(h)))
+        check(lib().fl_batch_create_parts(
+            k, ptr(sites), arr(u32p, [m.row_ptr for m in ms]), arr(u32p, [m.col for m in ms]),
+            arr(f64p, [m.length for m in ms]), arr(f64p, [m.area for m in ms]), ptr(ndef),
+            arr(u32p, [m.default_outlets for m in ms]),
+            arr(f64p, [m.xs for m in ms]) if have_xy else None,
+            arr(f64p, [m.ys for m in ms]) if have_xy else None, ctypes.byref(h)))
         self._handle = h
         return h
 
@@ -119,22 +110,28 @@ class BatchGenerator:
               for p in self.parameters]
         if len(ps) != b.num_terrains() or any(len(p) != m.num() for p, m in zip(ps, b.models)):
             raise GenerationError("InvalidNumberOfParameters")
-        cat = lambda f: np.ascontiguousarray(np.concatenate([getattr(p, f) for p in ps]))
-        base, k, u = cat("base"), cat("erodibility"), cat("uplift")
-        outl = np.ascontiguousarray(np.concatenate([p.is_outlet for p in ps]), np.uint8)
-        slopes = None
-        if any(p.max_slope is not None for p in ps):
-            slopes = np.ascontiguousarray(np.concatenate(
-                [p.max_slope if p.max_slope is not None else np.full(len(p), np.nan) for p in ps]))
-        out = np.empty(b.n, np.float64)
-        t_iters = np.zeros(b.num_terrains(), np.uint32)
+        k = b.num_terrains()
+        f64p = ctypes.POINTER(ctypes.c_double)
+        u8p = ctypes.POINTER(ctypes.c_uint8)
+        # the arrays stay referenced here while the call reads them
+        keep = [[np.ascontiguousarray(getattr(p, f), dt) for p in ps]
+                for f, dt in (("base", np.float64), ("erodibility", np.float64),
+                              ("uplift", np.float64), ("is_outlet", np.uint8))]
+        keep_slope = [None if p.max_slope is None else np.ascontiguousarray(p.max_slope, np.float64)
+                      for p in ps]
+        arr = lambda ctype, xs: (ctype * k)(*[None if x is None else x.ctypes.data_as(ctype)
+                                              for x in xs])
+        slopes = arr(f64p, keep_slope) if any(x is not None for x in keep_slope) else None
+        outs = [np.empty(m.num(), np.float64) for m in b.models]
+        t_iters = np.zeros(k, np.uint32)
         iters = ctypes.c_uint32()
         loop_ms, total_ms = ctypes.c_double(), ctypes.c_double()
         mi = -1 if self.max_iteration is None else self.max_iteration
-        rc = lib().fl_batch_generate(b.handle(), b.n, ptr(base), ptr(k), ptr(u), ptr(outl),
-                                     ptr(slopes) if slopes is not None else None, mi, ptr(out),
-                                     ptr(t_iters), ctypes.byref(iters), ctypes.byref(loop_ms),
-                                     ctypes.byref(total_ms))
+        rc = lib().fl_batch_generate_parts(
+            b.handle(), arr(f64p, keep[0]), arr(f64p, keep[1]), arr(f64p, keep[2]),
+            arr(u8p, keep[3]), slopes, mi,
+            arr(f64p, outs), ptr(t_iters), ctypes.byref(iters), ctypes.byref(loop_ms),
+            ctypes.byref(total_ms))
         if rc in _GEN_ERR:
             raise GenerationError(_GEN_ERR[rc])
         check(rc)
@@ -142,8 +139,4 @@ class BatchGenerator:
         self.last_iterations = iters.value
         self.last_loop_ms = loop_ms.value
         self.last_total_ms = total_ms.value
-        res = []
-        for t, m in enumerate(b.models):
-            a, e = int(b.site_off[t]), int(b.site_off[t + 1])
-            res.append(m.create_terrain_from_result(out[a:e].copy()))
-        return res
+        return [m.create_terrain_from_result(o) for m, o in zip(b.models, outs)]

@@ -233,6 +233,15 @@ void launch_inv_len(cudaStream_t st, uint64_t nnz, const double* len, float* ile
 // A model as the caller gives it (host arrays; site_off has terrains + 1 offsets) and
 // the device arrays ordering.cu fills in memory order (tid / noise_idx only for packed
 // terrains).
+// One terrain's arrays in its own site numbering (its row_ptr starts at 0).
+struct GraphPart {
+    const uint32_t* row_ptr;
+    const uint32_t* col;
+    const double* len;
+    const double* area;
+    const double* xs;
+    const double* ys;
+};
 struct GraphInput {
     uint32_t n;
     uint64_t nnz;
@@ -244,6 +253,8 @@ struct GraphInput {
     const double* ys;
     uint32_t terrains;
     const uint32_t* site_off;
+    const GraphPart* parts;   // instead of the arrays above: one part per terrain
+    const uint64_t* slot_off; // with parts: first slot of every terrain (terrains + 1)
 };
 struct GraphOutput {
     uint32_t* row;

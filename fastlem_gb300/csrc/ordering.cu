@@ -49,6 +49,25 @@ __device__ __forceinline__ uint32_t terrain_of(uint32_t i, const uint32_t* so, u
     return lo;
 }
 
+// Parts uploaded one after another: row entries and columns move by the part's first
+// slot and first site.
+__global__ void k_shift_parts(uint32_t n, uint64_t nnz, const uint32_t* __restrict__ so,
+                              const unsigned long long* __restrict__ eo, uint32_t k,
+                              uint32_t* __restrict__ row, uint32_t* __restrict__ col) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+        row[i] += (uint32_t)eo[terrain_of((uint32_t)i, so, k)];
+    for (uint64_t sl = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; sl < nnz; sl += stride) {
+        uint32_t lo = 0, hi = k;                         // eo[lo] <= sl < eo[hi]
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (eo[mid] <= sl) lo = mid;
+            else hi = mid;
+        }
+        col[sl] += so[lo];
+    }
+}
+
 __global__ void k_check_rows(uint32_t n, const uint32_t* __restrict__ row, uint32_t* st) {
     bool bad = false;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -186,13 +205,33 @@ int build_device_graph(cudaStream_t st, const GraphInput& in, const GraphOutput&
     uint32_t* so = tmp.get<uint32_t>(k + 1ull);
     uint32_t* st_w = tmp.get<uint32_t>(kCheckWords);
     if (!st_w) return cuda_fail(tmp.err, "graph upload");
-    OB_CU(cudaMemcpyAsync(row, in.row_ptr, (n + 1ull) * 4, cudaMemcpyHostToDevice, st), "graph upload");
-    if (nnz) {
-        OB_CU(cudaMemcpyAsync(col, in.col, nnz * 4, cudaMemcpyHostToDevice, st), "graph upload");
-        OB_CU(cudaMemcpyAsync(len, in.len, nnz * 8, cudaMemcpyHostToDevice, st), "graph upload");
-    }
-    OB_CU(cudaMemcpyAsync(area, in.area, n * 8ull, cudaMemcpyHostToDevice, st), "graph upload");
     OB_CU(cudaMemcpyAsync(so, in.site_off, (k + 1ull) * 4, cudaMemcpyHostToDevice, st), "graph upload");
+    const uint32_t nnz32 = (uint32_t)nnz;
+    if (!in.parts) {
+        OB_CU(cudaMemcpyAsync(row, in.row_ptr, (n + 1ull) * 4, cudaMemcpyHostToDevice, st), "graph upload");
+        if (nnz) {
+            OB_CU(cudaMemcpyAsync(col, in.col, nnz * 4, cudaMemcpyHostToDevice, st), "graph upload");
+            OB_CU(cudaMemcpyAsync(len, in.len, nnz * 8, cudaMemcpyHostToDevice, st), "graph upload");
+        }
+        OB_CU(cudaMemcpyAsync(area, in.area, n * 8ull, cudaMemcpyHostToDevice, st), "graph upload");
+    } else {
+        unsigned long long* eo = tmp.get<unsigned long long>(k + 1ull);
+        if (!eo) return cuda_fail(tmp.err, "graph upload");
+        for (uint32_t t = 0; t < k; ++t) {
+            const GraphPart& pt = in.parts[t];
+            const uint32_t a = in.site_off[t], m = in.site_off[t + 1] - a;
+            const uint64_t e0 = in.slot_off[t], ne = in.slot_off[t + 1] - e0;
+            OB_CU(cudaMemcpyAsync(row + a, pt.row_ptr, m * 4ull, cudaMemcpyHostToDevice, st), "graph upload");
+            if (ne) {
+                OB_CU(cudaMemcpyAsync(col + e0, pt.col, ne * 4, cudaMemcpyHostToDevice, st), "graph upload");
+                OB_CU(cudaMemcpyAsync(len + e0, pt.len, ne * 8, cudaMemcpyHostToDevice, st), "graph upload");
+            }
+            OB_CU(cudaMemcpyAsync(area + a, pt.area, m * 8ull, cudaMemcpyHostToDevice, st), "graph upload");
+        }
+        OB_CU(cudaMemcpyAsync(row + n, &nnz32, 4, cudaMemcpyHostToDevice, st), "graph upload");
+        OB_CU(cudaMemcpyAsync(eo, in.slot_off, (k + 1ull) * 8, cudaMemcpyHostToDevice, st), "graph upload");
+        k_shift_parts<<<grid_for(std::max<uint64_t>(n, nnz)), 256, 0, st>>>(n, nnz, so, eo, k, row, col);
+    }
     OB_CU(cudaMemsetAsync(st_w, 0, kCheckWords * 4, st), "graph upload");
     k_check_rows<<<grid_for(n), 256, 0, st>>>(n, row, st_w);
     uint32_t h[kCheckWords];
@@ -214,7 +253,8 @@ int build_device_graph(cudaStream_t st, const GraphInput& in, const GraphOutput&
         return 20;
     }
     // the memory order: per-terrain curve keys sorted stably (ties keep index order)
-    if (in.xs && in.ys) {
+    const bool coords = in.parts ? (in.parts[0].xs && in.parts[0].ys) : (in.xs && in.ys);
+    if (coords) {
         double* xs = tmp.get<double>(n);
         double* ys = tmp.get<double>(n);
         double* box = tmp.get<double>(4ull * k);
@@ -222,16 +262,31 @@ int build_device_graph(cudaStream_t st, const GraphInput& in, const GraphOutput&
         unsigned long long* key2 = tmp.get<unsigned long long>(n);
         uint32_t* val = tmp.get<uint32_t>(n);
         if (!val) return cuda_fail(tmp.err, "memory order");
-        OB_CU(cudaMemcpyAsync(xs, in.xs, n * 8ull, cudaMemcpyHostToDevice, st), "graph upload");
-        OB_CU(cudaMemcpyAsync(ys, in.ys, n * 8ull, cudaMemcpyHostToDevice, st), "graph upload");
+        for (uint32_t t = 0; t < k; ++t) {
+            const uint32_t a = in.site_off[t], m = in.site_off[t + 1] - a;
+            const double* px = in.parts ? in.parts[t].xs : in.xs + a;
+            const double* py = in.parts ? in.parts[t].ys : in.ys + a;
+            if (in.parts && (!px || !py)) {
+                *err = "coordinates given for some terrains only";
+                return 20;
+            }
+            if (in.parts || t == 0) {
+                const uint32_t cnt = in.parts ? m : n;
+                OB_CU(cudaMemcpyAsync(xs + a, px, cnt * 8ull, cudaMemcpyHostToDevice, st), "graph upload");
+                OB_CU(cudaMemcpyAsync(ys + a, py, cnt * 8ull, cudaMemcpyHostToDevice, st), "graph upload");
+            }
+        }
         // every terrain's bounding box (finite coordinates) on the host meanwhile
         std::vector<double> hb(4ull * k);
         const double cells = (double)((1u << kOrder) - 1);
         for (uint32_t t = 0; t < k; ++t) {
             double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
-            for (uint32_t i = in.site_off[t]; i < in.site_off[t + 1]; ++i) {
-                if (std::isfinite(in.xs[i])) { x0 = std::min(x0, in.xs[i]); x1 = std::max(x1, in.xs[i]); }
-                if (std::isfinite(in.ys[i])) { y0 = std::min(y0, in.ys[i]); y1 = std::max(y1, in.ys[i]); }
+            const uint32_t a = in.site_off[t], m = in.site_off[t + 1] - a;
+            const double* px = in.parts ? in.parts[t].xs : in.xs + a;
+            const double* py = in.parts ? in.parts[t].ys : in.ys + a;
+            for (uint32_t i = 0; i < m; ++i) {
+                if (std::isfinite(px[i])) { x0 = std::min(x0, px[i]); x1 = std::max(x1, px[i]); }
+                if (std::isfinite(py[i])) { y0 = std::min(y0, py[i]); y1 = std::max(y1, py[i]); }
             }
             hb[4 * t] = x0;
             hb[4 * t + 1] = y0;

@@ -12,6 +12,10 @@
 //     worker is free and its instance is idle or fits the HBM budget, after evicting
 //     idle instances (least recently used first); requests behind it wait, so a large
 //     request is never starved by smaller ones;
+//   * continuous batching: a request on a small model without a resident instance is
+//     solved together with the other such requests waiting at that moment, as one
+//     packed model (the batched form, every terrain keeping its own semantics), so the
+//     many small solves of a burst of arrivals cost about one;
 //   * each request records its queueing time, solve time and latency.
 // A request's result is exactly fl_generate's on its own: instances share nothing.
 
@@ -85,7 +89,9 @@ struct fl_server {
     bool stop = false;
     // statistics
     uint32_t active = 0, peak_active = 0;
-    uint64_t peak_used = 0, created = 0, evicted = 0, completed = 0;
+    uint64_t peak_used = 0, created = 0, evicted = 0, completed = 0, packs = 0,
+             packed_requests = 0;
+    bool pack = true;                   // continuous batching into packed solves
 };
 
 namespace {
@@ -104,6 +110,12 @@ void drop_idle(fl_server* s, uint32_t model, fl_graph* g) {
 }
 
 enum Admission { kWait = 0, kAdmit, kNever };
+
+// Continuous batching: requests on models of up to kPackMaxSites sites that find no
+// resident instance share packed solves of up to kPackMaxTotal sites.
+constexpr uint32_t kPackMaxSites = 1u << 21;
+constexpr uint64_t kPackMaxTotal = 24ull << 20;
+constexpr size_t kPackMaxRequests = 256;
 
 // With the lock held: can the head request start now?  Takes an idle instance
 // (*inst) or reserves budget for a new one (*reserve), evicting idle instances of
@@ -138,6 +150,94 @@ Admission admit(fl_server* s, Request* r, fl_graph** inst, uint64_t* reserve,
     return kAdmit;
 }
 
+// With the lock held, the head request r taking no idle instance: the waiting requests
+// that can share one packed solve with it (continuous batching into the batched form):
+// small models without an idle instance, the same iteration limit, in arrival order up
+// to the pack's site budget.  Reserves the packed model's device bytes (evicting idle
+// instances, least recently used first); returns the pack (r first) or an empty list
+// when it does not fit the budget now.
+std::vector<Request*> admit_pack(fl_server* s, Request* r, uint64_t* reserve,
+                                 std::vector<fl_graph*>* evict) {
+    std::vector<Request*> pack{r};
+    uint64_t sites = s->models[r->model]->n, slots = s->models[r->model]->col.size();
+    for (Request* q : s->queue) {
+        if (q == r || pack.size() >= kPackMaxRequests) continue;
+        const Model& m = *s->models[q->model];
+        if (!m.idle.empty() || m.n > kPackMaxSites || q->max_iter != r->max_iter ||
+            sites + m.n > kPackMaxTotal)
+            continue;
+        pack.push_back(q);
+        sites += m.n;
+        slots += m.col.size();
+    }
+    if (pack.size() < 2) return {};
+    const uint64_t need = fl_model_device_bytes((uint32_t)sites, slots);
+    uint64_t freeable = 0;
+    for (auto& e : s->lru) freeable += s->models[e.first]->bytes;
+    if (need > s->budget || s->used + need > s->budget + freeable) return {};
+    while (s->used + need > s->budget && !s->lru.empty()) {
+        auto e = s->lru.front();
+        s->lru.pop_front();
+        auto& v = s->models[e.first]->idle;
+        v.erase(std::remove(v.begin(), v.end(), e.second), v.end());
+        s->used -= s->models[e.first]->bytes;
+        evict->push_back(e.second);
+        s->evicted++;
+    }
+    s->used += need;
+    *reserve = need;
+    return pack;
+}
+
+// Solves a pack as one packed model (fl_batch_create_parts / fl_batch_generate_parts):
+// every terrain keeps its own semantics, so each result equals its solo generate().
+int solve_pack(fl_server* s, const std::vector<Request*>& pack, std::string* err) {
+    const size_t k = pack.size();
+    std::vector<uint32_t> sites(k), ndef(k);
+    std::vector<const uint32_t*> rows(k), cols(k), defs(k);
+    std::vector<const double*> lens(k), areas(k), xs(k), ys(k), base(k), kk(k), uu(k), slope(k);
+    std::vector<const uint8_t*> outl(k);
+    std::vector<double*> outs(k);
+    bool coords = true, any_slope = false;
+    for (size_t t = 0; t < k; ++t) {
+        const Model& m = *s->models[pack[t]->model];
+        const Request& q = *pack[t];
+        sites[t] = m.n;
+        ndef[t] = (uint32_t)m.outlets.size();
+        rows[t] = m.row.data();
+        cols[t] = m.col.data();
+        lens[t] = m.len.data();
+        areas[t] = m.area.data();
+        defs[t] = m.outlets.data();
+        coords = coords && m.coords;
+        xs[t] = m.coords ? m.xs.data() : nullptr;
+        ys[t] = m.coords ? m.ys.data() : nullptr;
+        base[t] = q.base.data();
+        kk[t] = q.k.data();
+        uu[t] = q.u.data();
+        outl[t] = q.outlet.data();
+        slope[t] = q.has_slope ? q.slope.data() : nullptr;
+        any_slope = any_slope || q.has_slope;
+        outs[t] = q.out;
+    }
+    fl_graph* g = nullptr;
+    int rc = fl_batch_create_parts((uint32_t)k, sites.data(), rows.data(), cols.data(), lens.data(),
+                                   areas.data(), ndef.data(), defs.data(),
+                                   coords ? xs.data() : nullptr, coords ? ys.data() : nullptr, &g);
+    if (rc == FL_OK) {
+        fl_graph_set_sized_grids(g, 1);
+        std::vector<uint32_t> titer(k, 0);
+        uint32_t iters = 0;
+        rc = fl_batch_generate_parts(g, base.data(), kk.data(), uu.data(), outl.data(),
+                                     any_slope ? slope.data() : nullptr, pack[0]->max_iter,
+                                     outs.data(), titer.data(), &iters, nullptr, nullptr);
+        for (size_t t = 0; t < k; ++t) pack[t]->iterations = titer[t];
+    }
+    if (rc != FL_OK) *err = fl_last_error();
+    fl_graph_destroy(g);
+    return rc;
+}
+
 void worker(fl_server* s) {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
@@ -146,15 +246,52 @@ void worker(fl_server* s) {
         fl_graph* inst = nullptr;
         uint64_t reserve = 0;
         std::vector<fl_graph*> evict;
+        std::vector<Request*> pack;
         bool never = false;
         s->cv_work.wait(lk, [&] {
             if (s->stop) return true;
             if (s->queue.empty()) return false;
-            const Admission a = admit(s, s->queue.front(), &inst, &reserve, &evict);
+            Request* h = s->queue.front();
+            const Model& hm = *s->models[h->model];
+            if (hm.idle.empty() && hm.n <= kPackMaxSites && s->pack) {
+                pack = admit_pack(s, h, &reserve, &evict);
+                if (!pack.empty()) return true;
+            }
+            const Admission a = admit(s, h, &inst, &reserve, &evict);
             never = a == kNever;
             return a != kWait;
         });
         if (s->stop) return;
+        if (!pack.empty()) {                    // a packed solve of several requests
+            for (Request* q : pack) {
+                s->queue.erase(std::find(s->queue.begin(), s->queue.end(), q));
+                s->models[q->model]->busy++;
+                q->started = Clock::now();
+            }
+            s->active++;
+            s->peak_active = std::max(s->peak_active, s->active);
+            s->packs++;
+            s->packed_requests += pack.size();
+            lk.unlock();
+            s->cv_work.notify_all();
+            for (fl_graph* g : evict) fl_graph_destroy(g);
+            std::string err;
+            const int rc = solve_pack(s, pack, &err);
+            lk.lock();
+            s->used -= reserve;
+            s->active--;
+            for (Request* q : pack) {
+                s->models[q->model]->busy--;
+                q->status = rc;
+                q->error = err;
+                q->finished = Clock::now();
+                q->done = true;
+                s->completed++;
+            }
+            s->cv_done.notify_all();
+            s->cv_work.notify_all();
+            continue;
+        }
         r = s->queue.front();
         s->queue.pop_front();
         if (never) {                          // fails alone; the requests behind it go on
@@ -344,8 +481,15 @@ int fl_server_stats(fl_server* s, uint64_t* out, uint32_t cap) {
     if (!s || !out) return FL_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(s->mu);
     const uint64_t v[] = {s->completed, s->peak_active, s->peak_used, s->used, s->created,
-                          s->evicted, (uint64_t)s->queue.size()};
+                          s->evicted, (uint64_t)s->queue.size(), s->packs, s->packed_requests};
     for (uint32_t i = 0; i < cap && i < sizeof v / sizeof v[0]; ++i) out[i] = v[i];
+    return FL_OK;
+}
+
+int fl_server_set_packing(fl_server* s, int enable) {
+    if (!s) return FL_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->pack = enable != 0;
     return FL_OK;
 }
 

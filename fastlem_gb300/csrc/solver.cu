@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -71,6 +72,15 @@ uint32_t kahn_min_width(uint32_t n, bool packed = false) {
 }
 
 thread_local std::string g_err;
+
+std::mutex& status_mu() {
+    static std::mutex m;
+    return m;
+}
+std::vector<int*>& status_free() {
+    static std::vector<int*> v;
+    return v;
+}
 
 void set_err(const char* what, cudaError_t e) {
     char buf[256];
@@ -460,15 +470,55 @@ struct fl_graph {
 
 namespace {
 
-// Device bytes allocated on this thread are added here while a model is being created.
+// Device bytes allocated on this thread are added here while a model is being created,
+// from the stream-ordered pool on its stream: creating or destroying a model then never
+// synchronises the device (solves of other models keep running).
 thread_local uint64_t* t_alloc_bytes = nullptr;
+thread_local cudaStream_t t_alloc_stream = nullptr;
+
+// Freed model memory stays in the device's pool for the next model (no release to the
+// driver, which would synchronise); set once per device.
+void keep_pool_memory() {
+    static std::mutex mu;
+    static std::vector<int> done;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), dev) != done.end()) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    done.push_back(dev);
+}
 
 template <class T>
 int dalloc(T** p, uint64_t count) {
     const uint64_t bytes = std::max<uint64_t>(1, count) * sizeof(T);
-    FL_CU(cudaMalloc((void**)p, bytes));
+    FL_CU(cudaMallocAsync((void**)p, bytes, t_alloc_stream));
     if (t_alloc_bytes) *t_alloc_bytes += bytes;
     return FL_OK;
+}
+
+// Page-locked 256-byte status blocks, recycled (freeing page-locked memory may
+// synchronise the device).
+int* status_block_get() {
+    std::lock_guard<std::mutex> lk(status_mu());
+    auto& fl = status_free();
+    if (!fl.empty()) {
+        int* b = fl.back();
+        fl.pop_back();
+        return b;
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, 256, cudaHostAllocPortable) != cudaSuccess) return nullptr;
+    return (int*)p;
+}
+void status_block_put(int* b) {
+    if (!b) return;
+    std::lock_guard<std::mutex> lk(status_mu());
+    status_free().push_back(b);
 }
 
 void free_graph(fl_graph* g) {
@@ -486,8 +536,8 @@ void free_graph(fl_graph* g) {
                     g->d_cpar1, g->d_cdep1, g->d_chist, g->d_corder, g->d_tokslot, g->d_pend,
                     g->d_corder_up, g->d_wa, g->d_wl, g->d_ilen, g->d_titer};
     for (void* p : ptrs)
-        if (p) cudaFree(p);
-    if (g->h_status) cudaFreeHost(g->h_status);
+        if (p) cudaFreeAsync(p, g->stream);
+    status_block_put(g->h_status);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
     for (auto& p : g->ev_pending) {
         cudaEventDestroy(p.second.first);
@@ -626,13 +676,17 @@ int alloc_workspace(fl_graph* g) {
     FL_TRY(dalloc(&g->d_td_done, n));
     // stamp-tagged words start below every stamp (stamps count from 1 per model, and
     // the memory may have belonged to an earlier model)
-    FL_CU(cudaMemset(g->d_bu_done, 0, n * 4ull));
-    FL_CU(cudaMemset(g->d_td_need, 0, n * 4ull));
-    FL_CU(cudaMemset(g->d_td_done, 0, n * 4ull));
-    FL_CU(cudaMemset(g->d_push, 0, n * 8ull));
-    FL_CU(cudaMemset(g->d_flags, 0, kNumFlags * 4ull));
-    FL_CU(cudaHostAlloc((void**)&g->h_status, (kNumFlags + kMetaCount) * sizeof(int),
-                        cudaHostAllocPortable));
+    FL_CU(cudaMemsetAsync(g->d_bu_done, 0, n * 4ull, g->stream));
+    FL_CU(cudaMemsetAsync(g->d_td_need, 0, n * 4ull, g->stream));
+    FL_CU(cudaMemsetAsync(g->d_td_done, 0, n * 4ull, g->stream));
+    FL_CU(cudaMemsetAsync(g->d_push, 0, n * 8ull, g->stream));
+    FL_CU(cudaMemsetAsync(g->d_flags, 0, kNumFlags * 4ull, g->stream));
+    static_assert((kNumFlags + kMetaCount) * sizeof(int) <= 256, "status block size");
+    g->h_status = status_block_get();
+    if (!g->h_status) {
+        g_err = "cudaHostAlloc failed";
+        return FL_ERR_OUT_OF_MEMORY;
+    }
     return FL_OK;
 }
 
@@ -673,23 +727,52 @@ int device_error(const int* h) {
 // Returned in device ids, list order unchanged (the order matters to the lake heap).
 // generator.rs:120-132, per terrain: the sites with is_outlet in ascending order, else
 // the terrain's default outlets (device ids, terrain after terrain).
-std::vector<uint32_t> resolve_outlets(const fl_graph* g, const uint8_t* is_outlet) {
+// A caller-order host array: one over all sites, or (packed terrains) one per terrain.
+template <class T>
+struct HostCols {
+    T* whole = nullptr;
+    T* const* parts = nullptr;
+    HostCols() = default;
+    HostCols(T* w) : whole(w) {}
+    static HostCols of_parts(T* const* p) {
+        HostCols c;
+        c.parts = p;
+        return c;
+    }
+    // every terrain has its array
+    bool complete(const fl_graph* g) const {
+        if (whole) return true;
+        if (!parts) return false;
+        for (uint32_t t = 0; t < g->terrains; ++t)
+            if (!parts[t]) return false;
+        return true;
+    }
+    bool any() const { return whole || parts; }
+    // terrain t's slice, indexed by its own site index (null when absent)
+    T* terrain(const fl_graph* g, uint32_t t) const {
+        if (whole) return whole + g->site_off[t];
+        return parts ? parts[t] : nullptr;
+    }
+};
+
+std::vector<uint32_t> resolve_outlets(const fl_graph* g, HostCols<const uint8_t> is_outlet) {
     std::vector<uint32_t> o;
     for (uint32_t t = 0; t < g->terrains; ++t) {
         const size_t first = o.size();
-        const uint32_t end = g->site_off[t + 1];
-        uint32_t i = g->site_off[t];
-        while (i < end) {
+        const uint8_t* a = is_outlet.terrain(g, t);
+        const uint32_t base = g->site_off[t], m = g->site_off[t + 1] - base;
+        uint32_t i = 0;
+        while (i < m) {
             // outlets are sparse: step over eight zero flags at a time
-            if (i + 8 <= end) {
+            if (i + 8 <= m) {
                 uint64_t word;
-                std::memcpy(&word, is_outlet + i, 8);
+                std::memcpy(&word, a + i, 8);
                 if (word == 0) {
                     i += 8;
                     continue;
                 }
             }
-            if (is_outlet[i]) o.push_back(g->inv[i]);
+            if (a[i]) o.push_back(g->inv[base + i]);
             ++i;
         }
         if (o.size() == first)
@@ -705,23 +788,43 @@ std::vector<uint32_t> to_device_ids(const fl_graph* g, const uint32_t* ids, uint
     return o;
 }
 
-// Uploads a caller-order f64 array into device order.
-int upload_permuted(fl_graph* g, const double* src, double* dst) {
-    FL_CU(cudaMemcpyAsync(g->d_t, src, g->n * 8ull, cudaMemcpyHostToDevice, g->stream));
+// Uploads a caller-order f64 array (whole or per terrain) into device order.
+int upload_permuted(fl_graph* g, HostCols<const double> src, double* dst) {
+    if (src.whole) {
+        FL_CU(cudaMemcpyAsync(g->d_t, src.whole, g->n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    } else {
+        for (uint32_t t = 0; t < g->terrains; ++t)
+            FL_CU(cudaMemcpyAsync(g->d_t + g->site_off[t], src.parts[t],
+                                  (g->site_off[t + 1] - g->site_off[t]) * 8ull,
+                                  cudaMemcpyHostToDevice, g->stream));
+    }
     k_gather_f64<<<blocks_for(g->n), kThreads, 0, g->stream>>>(g->n, g->d_perm, g->d_t, dst);
     FL_CU(cudaGetLastError());
     return FL_OK;
 }
+int upload_permuted(fl_graph* g, const double* src, double* dst) {
+    return upload_permuted(g, HostCols<const double>(src), dst);
+}
 
-// Downloads a device-order f64 array into caller order.
-int download_permuted(fl_graph* g, const double* src, double* dst) {
+// Downloads a device-order f64 array into caller order (whole or per terrain).
+int download_permuted(fl_graph* g, const double* src, HostCols<double> dst) {
     // w is dead after a pass (and response times must survive the downloads)
     double* stage = (src == g->d_w) ? g->d_t : g->d_w;
     if (stage == g->d_w) g->w_valid = false;
     k_gather_f64<<<blocks_for(g->n), kThreads, 0, g->stream>>>(g->n, g->d_inv, src, stage);
     FL_CU(cudaGetLastError());
-    FL_CU(cudaMemcpyAsync(dst, stage, g->n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    if (dst.whole) {
+        FL_CU(cudaMemcpyAsync(dst.whole, stage, g->n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    } else {
+        for (uint32_t t = 0; t < g->terrains; ++t)
+            FL_CU(cudaMemcpyAsync(dst.parts[t], stage + g->site_off[t],
+                                  (g->site_off[t + 1] - g->site_off[t]) * 8ull,
+                                  cudaMemcpyDeviceToHost, g->stream));
+    }
     return FL_OK;
+}
+int download_permuted(fl_graph* g, const double* src, double* dst) {
+    return download_permuted(g, src, HostCols<double>(dst));
 }
 
 // The model's CSR (device order) on the host, for the host heap and the probes;
@@ -1109,22 +1212,30 @@ int finish_basin_pass(fl_graph* g, const int* h) {
 // taken its data by the time it returns, so no host synchronisation is needed.
 // tan(max_slope) is computed on the host with the C library's tan, as fastlem's
 // `max_slope.tan()` is; without any slope limit the device array is just NaN.
-int upload_params(fl_graph* g, const double* base, const double* k, const double* u,
-                  const double* max_slope) {
+int upload_params(fl_graph* g, HostCols<const double> base, HostCols<const double> k,
+                  HostCols<const double> u, HostCols<const double> max_slope) {
     uint32_t n = g->n;
     g->slope = false;
-    if (base) FL_TRY(upload_permuted(g, base, g->d_base));
-    if (k) {
+    if (base.any()) FL_TRY(upload_permuted(g, base, g->d_base));
+    if (k.any()) {
         FL_TRY(upload_permuted(g, k, g->d_k));
         g->w_valid = false;
     }
-    if (u) FL_TRY(upload_permuted(g, u, g->d_u));
-    if (max_slope)
-        for (uint32_t i = 0; i < n && !g->slope; ++i) g->slope = !std::isnan(max_slope[i]);
+    if (u.any()) FL_TRY(upload_permuted(g, u, g->d_u));
+    // a terrain without max_slope array has no slope limit
+    for (uint32_t t = 0; t < g->terrains && !g->slope; ++t) {
+        const double* ms = max_slope.terrain(g, t);
+        const uint32_t m = g->site_off[t + 1] - g->site_off[t];
+        for (uint32_t i = 0; ms && i < m && !g->slope; ++i) g->slope = !std::isnan(ms[i]);
+    }
     if (g->slope) {
-        std::vector<double> tanv(n);
-        for (uint32_t i = 0; i < n; ++i)
-            tanv[i] = std::isnan(max_slope[i]) ? NAN : std::tan(max_slope[i]);
+        std::vector<double> tanv(n, NAN);
+        for (uint32_t t = 0; t < g->terrains; ++t) {
+            const double* ms = max_slope.terrain(g, t);
+            const uint32_t a = g->site_off[t], m = g->site_off[t + 1] - a;
+            for (uint32_t i = 0; ms && i < m; ++i)
+                tanv[a + i] = std::isnan(ms[i]) ? NAN : std::tan(ms[i]);
+        }
         FL_TRY(upload_permuted(g, tanv.data(), g->d_tan));
     } else {
         k_fill_nan<<<blocks_for(n), kThreads, 0, g->stream>>>(n, g->d_tan);
@@ -1133,15 +1244,17 @@ int upload_params(fl_graph* g, const double* base, const double* k, const double
     return FL_OK;
 }
 
-int generate_impl(fl_graph* g, uint32_t n_params, const double* base, const double* k,
-                  const double* u, const uint8_t* is_outlet, const double* max_slope,
-                  int64_t max_iter, double* out_elev, uint32_t* out_iters, double* loop_ms,
-                  double* total_ms, uint32_t* terrain_iters = nullptr) {
+int generate_impl(fl_graph* g, uint32_t n_params, HostCols<const double> base,
+                  HostCols<const double> k, HostCols<const double> u,
+                  HostCols<const uint8_t> is_outlet, HostCols<const double> max_slope,
+                  int64_t max_iter, HostCols<double> out_elev, uint32_t* out_iters,
+                  double* loop_ms, double* total_ms, uint32_t* terrain_iters = nullptr) {
     g_err.clear();
     if (!g) return FL_ERR_MODEL_NOT_SET;
-    if (!base || !k || !u || !is_outlet) return FL_ERR_PARAMETERS_NOT_SET;
+    if (!base.complete(g) || !k.complete(g) || !u.complete(g) || !is_outlet.complete(g))
+        return FL_ERR_PARAMETERS_NOT_SET;
     if (n_params != g->n) return FL_ERR_INVALID_NUM_PARAMETERS;
-    if (!out_elev) return FL_ERR_INVALID_ARGUMENT;
+    if (!out_elev.complete(g)) return FL_ERR_INVALID_ARGUMENT;
     FL_CU(cudaSetDevice(g->device));
     auto t_start = std::chrono::steady_clock::now();
     uint32_t n = g->n;
@@ -1252,10 +1365,11 @@ namespace {
 int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const double* len,
                  const double* area, const uint32_t* default_outlets, uint32_t n_default,
                  const double* xs, const double* ys, uint32_t k_terr, const uint32_t* site_off,
-                 const uint32_t* def_off, fl_graph** out) {
+                 const uint32_t* def_off, fl_graph** out, const fl::GraphPart* parts = nullptr) {
     g_err.clear();
-    if (!out || !row_ptr || (!col && n) || (!len && n) || !area || (n_default && !default_outlets) || n == 0 ||
-        n >= kNone || k_terr == 0 || (k_terr > 1 && (!site_off || !def_off))) {
+    if (!out || (!parts && (!row_ptr || (!col && n) || (!len && n) || !area)) ||
+        (n_default && !default_outlets) || n == 0 || n >= kNone || k_terr == 0 ||
+        (k_terr > 1 && (!site_off || !def_off))) {
         g_err = "invalid graph arguments";
         return FL_ERR_INVALID_ARGUMENT;
     }
@@ -1279,8 +1393,25 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
                 return FL_ERR_INVALID_ARGUMENT;
             }
     }
-    const uint64_t nnz = row_ptr[n];
-    if (row_ptr[0] != 0) { g_err = "row_ptr[0] != 0"; return FL_ERR_INVALID_ARGUMENT; }
+    std::vector<uint64_t> eo;                 // with parts: every terrain's first slot
+    uint64_t nnz = 0;
+    if (parts) {
+        eo.assign(k_terr + 1, 0);
+        for (uint32_t t = 0; t < k_terr; ++t) {
+            const fl::GraphPart& pt = parts[t];
+            const uint32_t m = so[t + 1] - so[t];
+            if (!pt.row_ptr || !pt.area || (pt.row_ptr[m] && (!pt.col || !pt.len))) {
+                g_err = "invalid graph arguments";
+                return FL_ERR_INVALID_ARGUMENT;
+            }
+            if (pt.row_ptr[0] != 0) { g_err = "row_ptr[0] != 0"; return FL_ERR_INVALID_ARGUMENT; }
+            eo[t + 1] = eo[t] + pt.row_ptr[m];
+        }
+        nnz = eo[k_terr];
+    } else {
+        nnz = row_ptr[n];
+        if (row_ptr[0] != 0) { g_err = "row_ptr[0] != 0"; return FL_ERR_INVALID_ARGUMENT; }
+    }
     if (nnz >= 0xffffffffull) { g_err = "more than 2^32 - 2 adjacency slots"; return FL_ERR_INVALID_ARGUMENT; }
     // default outlets: in their terrain, not repeated (the rest is checked on the device)
     for (uint32_t t = 0; t < k_terr; ++t) {
@@ -1301,8 +1432,12 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
     g->terrains = k_terr;
     struct Track {
         explicit Track(uint64_t* b) { t_alloc_bytes = b; }
-        ~Track() { t_alloc_bytes = nullptr; }
+        ~Track() {
+            t_alloc_bytes = nullptr;
+            t_alloc_stream = nullptr;
+        }
     } track(&g->dev_bytes);
+    keep_pool_memory();
     g->site_off = so;
     g->def_off = dof;
     for (uint32_t t = 0; t < k_terr; ++t) g->noise_n = std::max(g->noise_n, so[t + 1] - so[t]);
@@ -1310,6 +1445,7 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
     auto fail = [&](int r) { free_graph(g); return r; };
     cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { set_err("cudaStreamCreate", e); return fail(FL_ERR_CUDA); }
+    t_alloc_stream = g->stream;
     if (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess) {
         g_err = "cudaEventCreate failed";
         return fail(FL_ERR_CUDA);
@@ -1325,7 +1461,8 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
         return fail(rc);
     // upload, check and relabel on the device
     fl::GraphInput gi{n, nnz, row_ptr, col, len, area, (xs && ys) ? xs : nullptr,
-                      (xs && ys) ? ys : nullptr, k_terr, so.data()};
+                      (xs && ys) ? ys : nullptr, k_terr, so.data(), parts,
+                      parts ? eo.data() : nullptr};
     fl::GraphOutput go{g->d_row, g->d_col, g->d_len, g->d_area, g->d_perm, g->d_inv, g->d_tid,
                        g->d_noise_idx};
     std::string why;
@@ -1371,6 +1508,49 @@ int fl_batch_create(uint32_t terrains, const uint32_t* site_off, const uint32_t*
     }
     return create_graph(site_off[terrains], row_ptr, col, len, area, default_outlets,
                         def_off[terrains], xs, ys, terrains, site_off, def_off, out);
+}
+
+int fl_batch_create_parts(uint32_t terrains, const uint32_t* sites,
+                          const uint32_t* const* row_ptr, const uint32_t* const* col,
+                          const double* const* len, const double* const* area,
+                          const uint32_t* n_default, const uint32_t* const* default_outlets,
+                          const double* const* xs, const double* const* ys, fl_graph** out) {
+    g_err.clear();
+    if (!sites || !row_ptr || !col || !len || !area || !n_default || !default_outlets ||
+        terrains == 0) {
+        g_err = "invalid batch arguments";
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<uint32_t> so(terrains + 1, 0), dof(terrains + 1, 0), defs;
+    std::vector<fl::GraphPart> parts(terrains);
+    for (uint32_t t = 0; t < terrains; ++t) {
+        if ((uint64_t)so[t] + sites[t] >= kNone || (n_default[t] && !default_outlets[t])) {
+            g_err = "invalid batch arguments";
+            return FL_ERR_INVALID_ARGUMENT;
+        }
+        so[t + 1] = so[t] + sites[t];
+        dof[t + 1] = dof[t] + n_default[t];
+        for (uint32_t i = 0; i < n_default[t]; ++i) defs.push_back(so[t] + default_outlets[t][i]);
+        parts[t] = fl::GraphPart{row_ptr[t], col[t], len[t], area[t], xs ? xs[t] : nullptr,
+                                 ys ? ys[t] : nullptr};
+    }
+    return create_graph(so[terrains], nullptr, nullptr, nullptr, nullptr, defs.data(),
+                        dof[terrains], nullptr, nullptr, terrains, so.data(), dof.data(), out,
+                        parts.data());
+}
+
+int fl_batch_generate_parts(fl_graph* g, const double* const* base,
+                            const double* const* erodibility, const double* const* uplift,
+                            const uint8_t* const* is_outlet, const double* const* max_slope,
+                            int64_t max_iteration, double* const* out_elev,
+                            uint32_t* out_terrain_iterations, uint32_t* out_iterations,
+                            double* loop_ms, double* total_ms) {
+    using D = HostCols<const double>;
+    return generate_impl(g, g ? g->n : 0, D::of_parts(base), D::of_parts(erodibility),
+                         D::of_parts(uplift), HostCols<const uint8_t>::of_parts(is_outlet),
+                         D::of_parts(max_slope), max_iteration,
+                         HostCols<double>::of_parts(out_elev), out_iterations, loop_ms, total_ms,
+                         out_terrain_iterations);
 }
 
 uint32_t fl_graph_num_terrains(const fl_graph* g) { return g ? g->terrains : 0; }

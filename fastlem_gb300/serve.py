@@ -75,7 +75,12 @@ class TerrainServer:
         return ticket.model.create_terrain_from_result(ticket.out), info
 
     STATS = ["completed", "peak_active", "peak_device_bytes", "device_bytes", "instances_created",
-             "instances_evicted", "waiting"]
+             "instances_evicted", "waiting", "packed_solves", "packed_requests"]
+
+    def set_packing(self, enable: bool):
+        """Continuous batching of small requests into packed solves (on by default)."""
+        check(lib().fl_server_set_packing(self._h, 1 if enable else 0))
+        return self
 
     def stats(self):
         out = np.zeros(len(self.STATS), np.uint64)

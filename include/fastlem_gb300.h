@@ -137,6 +137,23 @@ int fl_batch_generate(fl_graph* g, uint32_t n_params, const double* base,
                       uint32_t* out_terrain_iterations, uint32_t* out_iterations,
                       double* loop_ms, double* total_ms);
 
+/* The same pair with every terrain's arrays passed separately, in its own site
+ * numbering (row_ptr[t] starts at 0, columns and default outlets are its own site
+ * ids): no concatenated copy is made.  xs / ys may be null (caller order kept), else
+ * every terrain has both.  max_slope may be null, and so may any of its entries (no
+ * slope limit on that terrain). */
+int fl_batch_create_parts(uint32_t terrains, const uint32_t* sites,
+                          const uint32_t* const* row_ptr, const uint32_t* const* col,
+                          const double* const* len, const double* const* area,
+                          const uint32_t* n_default, const uint32_t* const* default_outlets,
+                          const double* const* xs, const double* const* ys, fl_graph** out);
+int fl_batch_generate_parts(fl_graph* g, const double* const* base,
+                            const double* const* erodibility, const double* const* uplift,
+                            const uint8_t* const* is_outlet, const double* const* max_slope,
+                            int64_t max_iteration, double* const* out_elev,
+                            uint32_t* out_terrain_iterations, uint32_t* out_iterations,
+                            double* loop_ms, double* total_ms);
+
 /* ---- served form (no fastlem counterpart: a request loop of generate() calls) ------
  *
  * Models are registered once (the server keeps a host copy); requests name a model
@@ -174,9 +191,15 @@ int fl_server_submit(fl_server* s, uint32_t model_id, const double* base,
 int fl_server_wait(fl_server* s, uint64_t ticket, uint32_t* out_iterations, double* latency_ms,
                    double* queue_ms, double* solve_ms);
 
-/* Up to `cap` counters: requests completed, peak concurrent requests, peak and current
- * device bytes of instances, instances created, instances evicted, requests waiting. */
+/* Up to `cap` counters: requests completed, peak concurrent solves, peak and current
+ * device bytes of instances, instances created, instances evicted, requests waiting,
+ * packed solves run, requests solved in them. */
 int fl_server_stats(fl_server* s, uint64_t* out, uint32_t cap);
+/* Continuous batching on (1, the default) or off (0): requests on models of up to
+ * 2,097,152 sites that find no resident instance are solved together with the other such
+ * requests waiting at that moment (same iteration limit, up to 25,165,824 sites) as one
+ * packed model; their results are those of their solo generate(). */
+int fl_server_set_packing(fl_server* s, int enable);
 
 /* Stops the workers after the requests they are running; waiting requests are
  * dropped (their out_elev is never written).  Frees every instance and the server:

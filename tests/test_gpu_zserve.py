@@ -1,5 +1,6 @@
 """Served form: requests run concurrently through fl_server_* must each return exactly
-what fl_generate returns for the same model and parameters alone -- including when a
+what fl_generate returns for the same model and parameters alone -- with continuous
+batching (waiting requests solved together as one packed model) or without, and when a
 small HBM budget forces instances to be evicted and re-created."""
 import math
 
@@ -32,8 +33,9 @@ def solo(m, p, cap):
     return g.generate().elevations(), g.last_iterations
 
 
-@pytest.mark.parametrize("budget_models,slots", [(None, 3), (2, 2)])
-def test_requests_in_the_mix_equal_alone(requests, budget_models, slots):
+@pytest.mark.parametrize("budget_models,slots,packing", [(None, 3, True), (2, 2, True),
+                                                          (None, 3, False), (2, 2, False)])
+def test_requests_in_the_mix_equal_alone(requests, budget_models, slots, packing):
     cap = 30
     want = [solo(m, p, cap) for m, p in requests]
     # room for `budget_models` of the largest instance (admission reserves the bound
@@ -43,6 +45,7 @@ def test_requests_in_the_mix_equal_alone(requests, budget_models, slots):
     assert real <= bound
     budget = 120 * 10**9 if budget_models is None else budget_models * bound
     with TerrainServer(hbm_budget_bytes=budget, slots=slots) as srv:
+        srv.set_packing(packing)
         ids = [srv.add_model(m) for m, _ in requests]
         # every model twice, interleaved: resident instances get reused
         order = list(range(len(requests))) * 2
@@ -55,6 +58,11 @@ def test_requests_in_the_mix_equal_alone(requests, budget_models, slots):
         assert info["iterations"] == wi
         assert info["latency_ms"] >= info["solve_ms"] >= 0
     assert stats["completed"] == len(order)
+    if not packing:
+        assert stats["packed_solves"] == 0
+    elif budget_models is None:
+        assert stats["packed_requests"] >= 2      # the burst shares packed solves
     if budget_models is not None:
-        assert stats["instances_evicted"] > 0
+        if not packing:
+            assert stats["instances_evicted"] > 0
         assert stats["peak_device_bytes"] <= budget
