@@ -270,6 +270,7 @@ void worker(fl_server* s) {
             }
             s->active++;
             s->peak_active = std::max(s->peak_active, s->active);
+            s->peak_used = std::max(s->peak_used, s->used);
             s->packs++;
             s->packed_requests += pack.size();
             lk.unlock();
