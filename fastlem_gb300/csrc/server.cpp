@@ -92,6 +92,7 @@ struct fl_server {
     uint64_t peak_used = 0, created = 0, evicted = 0, completed = 0, packs = 0,
              packed_requests = 0;
     bool pack = true;                   // continuous batching into packed solves
+    uint32_t active_packs = 0;
 };
 
 namespace {
@@ -116,6 +117,7 @@ enum Admission { kWait = 0, kAdmit, kNever };
 constexpr uint32_t kPackMaxSites = 1u << 21;
 constexpr uint64_t kPackMaxTotal = 24ull << 20;
 constexpr size_t kPackMaxRequests = 256;
+constexpr uint32_t kMaxPacks = 2;               // packed solves running at a time
 
 // With the lock held: can the head request start now?  Takes an idle instance
 // (*inst) or reserves budget for a new one (*reserve), evicting idle instances of
@@ -150,12 +152,18 @@ Admission admit(fl_server* s, Request* r, fl_graph** inst, uint64_t* reserve,
     return kAdmit;
 }
 
-// With the lock held, the head request r taking no idle instance: the waiting requests
+// A request solved in a pack: packing on, a small model, no resident instance to reuse.
+bool packable(const fl_server* s, const Request* q) {
+    const Model& m = *s->models[q->model];
+    return s->pack && m.idle.empty() && m.n <= kPackMaxSites;
+}
+
+// With the lock held, the first packable request r: the waiting requests
 // that can share one packed solve with it (continuous batching into the batched form):
 // small models without an idle instance, the same iteration limit, in arrival order up
 // to the pack's site budget.  Reserves the packed model's device bytes (evicting idle
-// instances, least recently used first); returns the pack (r first) or an empty list
-// when it does not fit the budget now.
+// instances, least recently used first); returns the pack (r first, possibly alone) or
+// an empty list when it does not fit the budget now.
 std::vector<Request*> admit_pack(fl_server* s, Request* r, uint64_t* reserve,
                                  std::vector<fl_graph*>* evict) {
     std::vector<Request*> pack{r};
@@ -163,14 +171,12 @@ std::vector<Request*> admit_pack(fl_server* s, Request* r, uint64_t* reserve,
     for (Request* q : s->queue) {
         if (q == r || pack.size() >= kPackMaxRequests) continue;
         const Model& m = *s->models[q->model];
-        if (!m.idle.empty() || m.n > kPackMaxSites || q->max_iter != r->max_iter ||
-            sites + m.n > kPackMaxTotal)
+        if (!packable(s, q) || q->max_iter != r->max_iter || sites + m.n > kPackMaxTotal)
             continue;
         pack.push_back(q);
         sites += m.n;
         slots += m.col.size();
     }
-    if (pack.size() < 2) return {};
     const uint64_t need = fl_model_device_bytes((uint32_t)sites, slots);
     uint64_t freeable = 0;
     for (auto& e : s->lru) freeable += s->models[e.first]->bytes;
@@ -251,15 +257,29 @@ void worker(fl_server* s) {
         s->cv_work.wait(lk, [&] {
             if (s->stop) return true;
             if (s->queue.empty()) return false;
-            Request* h = s->queue.front();
-            const Model& hm = *s->models[h->model];
-            if (hm.idle.empty() && hm.n <= kPackMaxSites && s->pack) {
-                pack = admit_pack(s, h, &reserve, &evict);
+            // small requests without a resident instance: packed solves, at most
+            // kMaxPacks at a time, each taking every such request waiting when it starts
+            // (the others keep arriving meanwhile and make the next pack larger)
+            Request* first_small = nullptr;
+            for (Request* q : s->queue)
+                if (packable(s, q)) {
+                    first_small = q;
+                    break;
+                }
+            if (first_small && s->active_packs < kMaxPacks) {
+                pack = admit_pack(s, first_small, &reserve, &evict);
                 if (!pack.empty()) return true;
             }
-            const Admission a = admit(s, h, &inst, &reserve, &evict);
-            never = a == kNever;
-            return a != kWait;
+            // everything else solo, in arrival order
+            for (Request* q : s->queue) {
+                if (packable(s, q)) continue;
+                const Admission a = admit(s, q, &inst, &reserve, &evict);
+                if (a == kWait) return false;
+                never = a == kNever;
+                r = q;
+                return true;
+            }
+            return false;
         });
         if (s->stop) return;
         if (!pack.empty()) {                    // a packed solve of several requests
@@ -269,6 +289,7 @@ void worker(fl_server* s) {
                 q->started = Clock::now();
             }
             s->active++;
+            s->active_packs++;
             s->peak_active = std::max(s->peak_active, s->active);
             s->peak_used = std::max(s->peak_used, s->used);
             s->packs++;
@@ -281,6 +302,7 @@ void worker(fl_server* s) {
             lk.lock();
             s->used -= reserve;
             s->active--;
+            s->active_packs--;
             for (Request* q : pack) {
                 s->models[q->model]->busy--;
                 q->status = rc;
@@ -293,8 +315,7 @@ void worker(fl_server* s) {
             s->cv_work.notify_all();
             continue;
         }
-        r = s->queue.front();
-        s->queue.pop_front();
+        s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
         if (never) {                          // fails alone; the requests behind it go on
             r->status = FL_ERR_OUT_OF_MEMORY;
             r->error = "fl_server: the model's instance is larger than the HBM budget";

@@ -28,6 +28,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -399,6 +400,7 @@ struct fl_graph {
     std::vector<uint32_t> h_rank;        // host-computed rank (empty when computed on the GPU)
     int rank_gpu = -1;                   // where the last rank was computed: 1 GPU, 0 host
     int sized_grids = -1;                // model-sized cooperative grids: -1 the schedule's
+    double* h_stage = nullptr;           // page-locked staging array (many packed terrains)
     double rank_ms = 0.0;                // its host wall time
     // device order: perm[device index] = caller index, inv the reverse
     std::vector<uint32_t> perm, inv;
@@ -538,6 +540,7 @@ void free_graph(fl_graph* g) {
     for (void* p : ptrs)
         if (p) cudaFreeAsync(p, g->stream);
     status_block_put(g->h_status);
+    if (g->h_stage) cudaFreeHost(g->h_stage);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
     for (auto& p : g->ev_pending) {
         cudaEventDestroy(p.second.first);
@@ -788,10 +791,41 @@ std::vector<uint32_t> to_device_ids(const fl_graph* g, const uint32_t* ids, uint
     return o;
 }
 
+// Many terrains' arrays pass through one page-locked staging array (one transfer instead
+// of one per terrain, each of which costs a fixed driver overhead).
+constexpr uint32_t kStageTerrains = 32;
+
+int host_stage(fl_graph* g) {
+    if (g->h_stage) return FL_OK;
+    FL_CU(cudaHostAlloc((void**)&g->h_stage, std::max<uint64_t>(1, g->n) * 8ull, cudaHostAllocPortable));
+    return FL_OK;
+}
+
+// Copies between the staging array and the terrains' arrays on a few host threads.
+template <class F>
+void per_terrain_threads(const fl_graph* g, F f) {
+    const unsigned nt = g->n < (1u << 20) ? 1u : std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned w = 1; w < nt; ++w)
+        th.emplace_back([&, w] {
+            for (uint32_t t = w; t < g->terrains; t += nt) f(t);
+        });
+    for (uint32_t t = 0; t < g->terrains; t += nt) f(t);
+    for (auto& x : th) x.join();
+}
+
 // Uploads a caller-order f64 array (whole or per terrain) into device order.
 int upload_permuted(fl_graph* g, HostCols<const double> src, double* dst) {
     if (src.whole) {
         FL_CU(cudaMemcpyAsync(g->d_t, src.whole, g->n * 8ull, cudaMemcpyHostToDevice, g->stream));
+    } else if (g->terrains > kStageTerrains) {
+        FL_TRY(host_stage(g));
+        FL_CU(cudaStreamSynchronize(g->stream));       // the previous staged copy is done
+        per_terrain_threads(g, [&](uint32_t t) {
+            std::memcpy(g->h_stage + g->site_off[t], src.parts[t],
+                        (g->site_off[t + 1] - g->site_off[t]) * 8ull);
+        });
+        FL_CU(cudaMemcpyAsync(g->d_t, g->h_stage, g->n * 8ull, cudaMemcpyHostToDevice, g->stream));
     } else {
         for (uint32_t t = 0; t < g->terrains; ++t)
             FL_CU(cudaMemcpyAsync(g->d_t + g->site_off[t], src.parts[t],
@@ -815,6 +849,14 @@ int download_permuted(fl_graph* g, const double* src, HostCols<double> dst) {
     FL_CU(cudaGetLastError());
     if (dst.whole) {
         FL_CU(cudaMemcpyAsync(dst.whole, stage, g->n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+    } else if (g->terrains > kStageTerrains) {
+        FL_TRY(host_stage(g));
+        FL_CU(cudaMemcpyAsync(g->h_stage, stage, g->n * 8ull, cudaMemcpyDeviceToHost, g->stream));
+        FL_CU(cudaStreamSynchronize(g->stream));
+        per_terrain_threads(g, [&](uint32_t t) {
+            std::memcpy(dst.parts[t], g->h_stage + g->site_off[t],
+                        (g->site_off[t + 1] - g->site_off[t]) * 8ull);
+        });
     } else {
         for (uint32_t t = 0; t < g->terrains; ++t)
             FL_CU(cudaMemcpyAsync(dst.parts[t], stage + g->site_off[t],
