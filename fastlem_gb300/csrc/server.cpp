@@ -158,29 +158,37 @@ bool packable(const fl_server* s, const Request* q) {
     return s->pack && m.idle.empty() && m.n <= kPackMaxSites;
 }
 
-// With the lock held, the first packable request r: the waiting requests
-// that can share one packed solve with it (continuous batching into the batched form):
-// small models without an idle instance, the same iteration limit, in arrival order up
-// to the pack's site budget.  Reserves the packed model's device bytes (evicting idle
-// instances, least recently used first); returns the pack (r first, possibly alone) or
-// an empty list when it does not fit the budget now.
-std::vector<Request*> admit_pack(fl_server* s, Request* r, uint64_t* reserve,
-                                 std::vector<fl_graph*>* evict) {
-    std::vector<Request*> pack{r};
-    uint64_t sites = s->models[r->model]->n, slots = s->models[r->model]->col.size();
+// With the lock held, the first packable request r: the waiting requests that can share
+// one packed solve with it (continuous batching into the batched form): packable, the
+// same iteration limit, in arrival order while the pack's site limit and the HBM budget
+// (idle instances counted as freeable) allow.  Reserves the packed model's device bytes,
+// evicting idle instances least recently used first.  kNever: r alone can never fit.
+Admission admit_pack(fl_server* s, Request* r, std::vector<Request*>* pack, uint64_t* reserve,
+                     std::vector<fl_graph*>* evict) {
+    pack->clear();
+    uint64_t freeable = 0;
+    for (auto& e : s->lru) freeable += s->models[e.first]->bytes;
+    const uint64_t room = s->budget + freeable > s->used ? s->budget + freeable - s->used : 0;
+    uint64_t sites = 0, slots = 0, need = 0;
     for (Request* q : s->queue) {
-        if (q == r || pack.size() >= kPackMaxRequests) continue;
+        if (pack->size() >= kPackMaxRequests) break;
         const Model& m = *s->models[q->model];
         if (!packable(s, q) || q->max_iter != r->max_iter || sites + m.n > kPackMaxTotal)
             continue;
-        pack.push_back(q);
+        const uint64_t nd = fl_model_device_bytes((uint32_t)(sites + m.n), slots + m.col.size());
+        if (nd > room) {
+            if (q == r) {
+                const uint64_t alone = fl_model_device_bytes(m.n, m.col.size());
+                return alone > s->budget ? kNever : kWait;
+            }
+            continue;
+        }
+        pack->push_back(q);
         sites += m.n;
         slots += m.col.size();
+        need = nd;
     }
-    const uint64_t need = fl_model_device_bytes((uint32_t)sites, slots);
-    uint64_t freeable = 0;
-    for (auto& e : s->lru) freeable += s->models[e.first]->bytes;
-    if (need > s->budget || s->used + need > s->budget + freeable) return {};
+    if (pack->empty()) return kWait;
     while (s->used + need > s->budget && !s->lru.empty()) {
         auto e = s->lru.front();
         s->lru.pop_front();
@@ -192,7 +200,7 @@ std::vector<Request*> admit_pack(fl_server* s, Request* r, uint64_t* reserve,
     }
     s->used += need;
     *reserve = need;
-    return pack;
+    return kAdmit;
 }
 
 // Solves a pack as one packed model (fl_batch_create_parts / fl_batch_generate_parts):
@@ -267,8 +275,14 @@ void worker(fl_server* s) {
                     break;
                 }
             if (first_small && s->active_packs < kMaxPacks) {
-                pack = admit_pack(s, first_small, &reserve, &evict);
-                if (!pack.empty()) return true;
+                const Admission a = admit_pack(s, first_small, &pack, &reserve, &evict);
+                if (a == kAdmit) return true;
+                if (a == kNever) {              // fails alone below
+                    pack.clear();
+                    never = true;
+                    r = first_small;
+                    return true;
+                }
             }
             // everything else solo, in arrival order
             for (Request* q : s->queue) {
