@@ -159,18 +159,22 @@ def peak_hbm():
 # so the 1M config's launch (8th iteration of a generate(), --set full) is scaled by
 # the units (traffic grows with them).
 NCU_TRAFFIC = {
-    # 52.31 MB over the 891,787 Kahn-region sites (1,000,000 - 108,213 skeleton sites)
-    "kahn_rounds": (52.306e6 / 891_787, "kahn_sites",
+    # 56.76 MB over the 939,485 Kahn-region sites (1,000,000 - 60,515 skeleton sites)
+    "kahn_rounds": (56.763e6 / 939_485, "kahn_sites",
                     "ncu dram__bytes_read+write of one k_kahn launch on the 1M config "
                     "(8th iteration), scaled by Kahn-region sites"),
-    # 6.421 MB over 108,213 skeleton sites
-    "skeleton_up": (6.421e6 / 108_213, "skeleton_sites",
+    # 3.064 MB over 60,515 skeleton sites
+    "skeleton_up": (3.064e6 / 60_515, "skeleton_sites",
                     "ncu dram__bytes_read+write of one k_s_bottom_up launch on the 1M config "
                     "(8th iteration), scaled by skeleton sites"),
-    # 113.20 MB over 1,000,000 sites
-    "receivers": (113.20e6 / 1_000_000, "sites",
+    # 113.38 MB over 1,000,000 sites
+    "receivers": (113.38e6 / 1_000_000, "sites",
                   "ncu dram__bytes_read+write of one k_receivers launch on the 1M config "
                   "(8th iteration), scaled by sites"),
+    # 52.40 MB over the 939,485 Kahn-region sites
+    "rounds_down": (52.40e6 / 939_485, "kahn_sites",
+                    "ncu dram__bytes_read+write of one k_low_top_down launch on the 1M config "
+                    "(8th iteration), scaled by Kahn-region sites"),
     # 39.41 MB over 1,000,000 sites
     "response_w": (39.41e6 / 1_000_000, "sites",
                    "ncu dram__bytes_read+write of one k_w launch on the 1M config "
