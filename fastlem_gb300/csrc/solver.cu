@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdlib>
 #include <cmath>
@@ -758,16 +759,34 @@ struct HostCols {
     }
 };
 
-std::vector<uint32_t> resolve_outlets(const fl_graph* g, HostCols<const uint8_t> is_outlet) {
-    std::vector<uint32_t> o;
-    for (uint32_t t = 0; t < g->terrains; ++t) {
-        const size_t first = o.size();
-        const uint8_t* a = is_outlet.terrain(g, t);
-        const uint32_t base = g->site_off[t], m = g->site_off[t + 1] - base;
-        uint32_t i = 0;
-        while (i < m) {
+// Runs f(lo, hi, w) over [0, m) cut into contiguous ranges, range w on host thread w:
+// one range below 2^20 elements, else up to eight.  Ranges come in index order, so
+// per-range results concatenated in w order are the serial scan's.
+constexpr unsigned kHostRanges = 8;
+template <class F>
+void host_ranges(uint32_t m, F f) {
+    const unsigned nt = m < (1u << 20) ? 1u
+                                       : std::max(1u, std::min(kHostRanges, std::thread::hardware_concurrency()));
+    const uint64_t step = (m + nt - 1) / nt;
+    auto range = [&](unsigned w) {
+        f((uint32_t)std::min<uint64_t>(m, w * step), (uint32_t)std::min<uint64_t>(m, (w + 1) * step), w);
+    };
+    std::vector<std::thread> th;
+    for (unsigned w = 1; w < nt; ++w) th.emplace_back(range, w);
+    range(0);
+    for (auto& x : th) x.join();
+}
+
+// Appends base-relative site i (as its device id) for every nonzero a[i], i ascending.
+void flagged_sites(const fl_graph* g, const uint8_t* a, uint32_t base, uint32_t m,
+                   std::vector<uint32_t>& o) {
+    std::vector<uint32_t> part[kHostRanges];
+    host_ranges(m, [&](uint32_t lo, uint32_t hi, unsigned w) {
+        std::vector<uint32_t>& out = w ? part[w] : o;
+        uint32_t i = lo;
+        while (i < hi) {
             // outlets are sparse: step over eight zero flags at a time
-            if (i + 8 <= m) {
+            if (i + 8 <= hi) {
                 uint64_t word;
                 std::memcpy(&word, a + i, 8);
                 if (word == 0) {
@@ -775,9 +794,33 @@ std::vector<uint32_t> resolve_outlets(const fl_graph* g, HostCols<const uint8_t>
                     continue;
                 }
             }
-            if (a[i]) o.push_back(g->inv[base + i]);
+            if (a[i]) out.push_back(g->inv[base + i]);
             ++i;
         }
+    });
+    for (unsigned w = 1; w < kHostRanges; ++w) o.insert(o.end(), part[w].begin(), part[w].end());
+}
+
+// Whether any of m max_slope entries is a number (NaN means no limit).
+bool any_slope_limit(const double* ms, uint32_t m) {
+    std::atomic<bool> found{false};
+    host_ranges(m, [&](uint32_t lo, uint32_t hi, unsigned) {
+        for (uint32_t a = lo; a < hi && !found.load(std::memory_order_relaxed); a += 4096) {
+            const uint32_t e = std::min(hi, a + 4096);
+            int num = 0;
+            for (uint32_t i = a; i < e; ++i) num |= ms[i] == ms[i];   // false for NaN only
+            if (num) found.store(true, std::memory_order_relaxed);
+        }
+    });
+    return found.load();
+}
+
+std::vector<uint32_t> resolve_outlets(const fl_graph* g, HostCols<const uint8_t> is_outlet) {
+    std::vector<uint32_t> o;
+    for (uint32_t t = 0; t < g->terrains; ++t) {
+        const size_t first = o.size();
+        const uint32_t base = g->site_off[t], m = g->site_off[t + 1] - base;
+        flagged_sites(g, is_outlet.terrain(g, t), base, m, o);
         if (o.size() == first)
             o.insert(o.end(), g->def_outlets.begin() + g->def_off[t],
                      g->def_outlets.begin() + g->def_off[t + 1]);
@@ -1267,16 +1310,17 @@ int upload_params(fl_graph* g, HostCols<const double> base, HostCols<const doubl
     // a terrain without max_slope array has no slope limit
     for (uint32_t t = 0; t < g->terrains && !g->slope; ++t) {
         const double* ms = max_slope.terrain(g, t);
-        const uint32_t m = g->site_off[t + 1] - g->site_off[t];
-        for (uint32_t i = 0; ms && i < m && !g->slope; ++i) g->slope = !std::isnan(ms[i]);
+        if (ms) g->slope = any_slope_limit(ms, g->site_off[t + 1] - g->site_off[t]);
     }
     if (g->slope) {
         std::vector<double> tanv(n, NAN);
         for (uint32_t t = 0; t < g->terrains; ++t) {
             const double* ms = max_slope.terrain(g, t);
             const uint32_t a = g->site_off[t], m = g->site_off[t + 1] - a;
-            for (uint32_t i = 0; ms && i < m; ++i)
-                tanv[a + i] = std::isnan(ms[i]) ? NAN : std::tan(ms[i]);
+            if (!ms) continue;
+            host_ranges(m, [&](uint32_t lo, uint32_t hi, unsigned) {
+                for (uint32_t i = lo; i < hi; ++i) tanv[a + i] = std::isnan(ms[i]) ? NAN : std::tan(ms[i]);
+            });
         }
         FL_TRY(upload_permuted(g, tanv.data(), g->d_tan));
     } else {
