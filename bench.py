@@ -39,7 +39,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="16m", choices=["small", "1m", "16m", "batched", "served"])
+    ap.add_argument("--config", default="16m",
+                    choices=["small", "1m", "16m", "batched", "served", "interp"])
+    ap.add_argument("--interp-sites", type=int, default=1_000_000,
+                    help="interp: sites of the terrain whose elevations are rendered")
+    ap.add_argument("--interp-grid", type=int, default=4096,
+                    help="interp: pixels per side of the rendering grid")
     ap.add_argument("--requests", type=int, default=64, help="served: requests in the stream")
     ap.add_argument("--slots", type=int, default=12, help="served: concurrent requests (worker threads)")
     ap.add_argument("--serve-iters", type=int, default=64,
@@ -488,6 +493,9 @@ def bench_gpu(args, d):
                                               "sequential_plain", "speedup_vs_sequential",
                                               "identical_to_plain", "cpu_baseline", "server")}
         line["served"]["config"] = sv["config"]
+        it = bench_interp(ea, d, emit=False)
+        line["interp"] = {k: it[k] for k in ("metric", "value", "unit", "e2e", "cpu_baseline",
+                                             "identical_to_host", "config")}
     print(json.dumps(line), flush=True)
 
 
@@ -685,6 +693,89 @@ def bench_served(args, d, emit=True):
     return line
 
 
+def bench_interp(args, d, emit=True):
+    """Terrain2D::get_elevation over a rendering grid (src/models/surface/terrain.rs:35-38,
+    the per-pixel loop of examples/landscape_evolution.rs at a larger size): a terrain of
+    random sites in [0,4000]^2 rendered on an n x n pixel grid covering the box.  value:
+    device-resident queries (fl_interpolate_device); e2e: host arrays in and out
+    (fl_interpolate_gpu); cpu_baseline: the host fl_interpolate on every core, on a band
+    of rows; identical_to_host: the two give the same bits on that band."""
+    import torch
+    from fastlem_gb300 import Site2D, TerrainModel2DBulider, build as fb
+    from fastlem_gb300 import _lib
+    from fastlem_gb300.api import TerrainInterpolator2D
+    fb.build()
+    _lib.check(_lib.lib().fl_select_device(d.local))
+    torch.cuda.set_device(d.local)
+    t0 = time.time()
+    model = TerrainModel2DBulider.from_random_sites(
+        args.interp_sites, Site2D(0.0, 0.0), Site2D(4000.0, 4000.0), seed=7).build()
+    elev = np.random.default_rng(7).uniform(0.0, 500.0, model.num())
+    it = TerrainInterpolator2D(model.xs, model.ys)
+    build_s = time.time() - t0
+    g = args.interp_grid
+    px = (np.arange(g, dtype=np.float64) + 0.5) * (4000.0 / g)
+    QX, QY = np.meshgrid(px, px)
+    qx, qy = np.ascontiguousarray(QX.ravel()), np.ascontiguousarray(QY.ravel())
+    count = qx.size
+    dev = torch.device("cuda", d.local)
+    tf, tx, ty = (torch.from_numpy(a).to(dev) for a in (elev, qx, qy))
+    out = torch.empty(count, dtype=torch.float64, device=dev)
+    found = torch.empty(count, dtype=torch.uint8, device=dev)
+    for _ in range(max(3, args.warmup)):
+        it.interpolate_device(tf, tx, ty, out, found)
+    steps = max(1, args.steps)
+    torch.cuda.synchronize()
+    d.barrier()
+    t = time.perf_counter()
+    for _ in range(steps):
+        it.interpolate_device(tf, tx, ty, out, found)
+    dev_s = (time.perf_counter() - t) / steps
+    host_out = _lib.pinned_empty(count, np.float64)
+    hx, hy = _lib.pinned_empty(count, np.float64), _lib.pinned_empty(count, np.float64)
+    hx[:], hy[:] = qx, qy
+    for _ in range(2):
+        v, ok = it.interpolate_many(elev, hx, hy, gpu=True)
+    t = time.perf_counter()
+    for _ in range(steps):
+        v, ok = it.interpolate_many(elev, hx, hy, gpu=True)
+    e2e_s = (time.perf_counter() - t) / steps
+    dev_vals = out.cpu().numpy()
+    # host baseline on a band of rows (about 10 s of host work at most)
+    rows = max(1, min(g, int(2_000_000 // g)))
+    band = slice((g // 2) * g, (g // 2 + rows) * g)
+    it.interpolate_many(elev, qx[:1000], qy[:1000])
+    t = time.perf_counter()
+    hv, hok = it.interpolate_many(elev, qx[band], qy[band])
+    cpu_s = time.perf_counter() - t
+    same = bool(np.array_equal(hv.view(np.uint64), dev_vals[band].view(np.uint64)) and
+                np.array_equal(hok, found.cpu().numpy()[band].astype(bool)) and
+                np.array_equal(v.view(np.uint64), dev_vals.view(np.uint64)))
+    cores = min(16, os.cpu_count() or 1)
+    line = {
+        "metric": f"natural-neighbour queries/s ({g}x{g} rendering grid, {model.num():,} sites)",
+        "value": count / dev_s / 1e6, "unit": "Mqueries/s", "n_gpus": 1,
+        "e2e": {"value": count / e2e_s / 1e6, "unit": "Mqueries/s",
+                "h2d_bytes_per_step": 16 * count + 8 * model.num(),
+                "d2h_bytes_per_step": 9 * count},
+        "cpu_baseline": {"value": (band.stop - band.start) / cpu_s / 1e6, "unit": "Mqueries/s",
+                         "cores": cores, "kind": "port",
+                         "sample": f"host fl_interpolate (the same construction on host threads) on "
+                                   f"{rows} middle rows of the grid ({band.stop - band.start:,} "
+                                   f"queries), {cpu_s:.2f} s"},
+        "identical_to_host": same,
+        "ms_per_step": dev_s * 1000, "e2e_ms_per_step": e2e_s * 1000,
+        "found_fraction": float(found.float().mean().item()),
+        "config": {"workload": f"interp: {model.num():,} random sites in [0,4000]^2 seed 7 "
+                               f"(from_random_sites), uniform(0,500) elevations, {g}x{g} pixel "
+                               f"centres", "queries_per_step": count, "steps": steps,
+                   "model_and_triangulation_build_s": round(build_s, 1)},
+    }
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
+
+
 def main():
     args = parse()
     d = Dist()
@@ -693,6 +784,9 @@ def main():
         return
     if args.config == "served" and args.impl != "reference":
         bench_served(args, d)
+        return
+    if args.config == "interp" and args.impl != "reference":
+        bench_interp(args, d)
         return
     if args.impl == "reference":
         bench_reference(args, d)

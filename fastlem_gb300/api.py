@@ -347,9 +347,10 @@ class TerrainInterpolator2D:
                                            ctypes.byref(h)))
         self._h = h
 
-    def interpolate_many(self, elevations, qx, qy):
+    def interpolate_many(self, elevations, qx, qy, gpu=False):
         """(values, found) for arrays of query coordinates; values are NaN where the
-        query lies outside the hull (found False)."""
+        query lies outside the hull (found False).  gpu=True answers them on the GPU
+        (fl_interpolate_gpu), with the same bits."""
         e = as_f64(elevations)
         if len(e) != len(self.xs):
             raise ValueError("one elevation per site")
@@ -358,9 +359,27 @@ class TerrainInterpolator2D:
             raise ValueError("qx and qy differ in shape")
         out = np.empty(qx.shape, np.float64)
         found = np.empty(qx.shape, np.uint8)
-        check(lib().fl_interpolate(self._h, ptr(e), qx.size, ptr(qx), ptr(qy), ptr(out),
-                                   ptr(found)))
+        call = lib().fl_interpolate_gpu if gpu else lib().fl_interpolate
+        check(call(self._h, ptr(e), qx.size, ptr(qx), ptr(qy), ptr(out), ptr(found)))
         return out, found.astype(bool)
+
+    def interpolate_device(self, elevations, qx, qy, out, found):
+        """fl_interpolate_device on torch CUDA tensors (float64 elevations, queries and
+        out, uint8 found), all on the device the interpolator uses."""
+        import torch
+        for name, t, dt in (("elevations", elevations, torch.float64), ("qx", qx, torch.float64),
+                            ("qy", qy, torch.float64), ("out", out, torch.float64),
+                            ("found", found, torch.uint8)):
+            if not (t.is_cuda and t.dtype == dt and t.is_contiguous()):
+                raise ValueError(f"{name}: a contiguous CUDA tensor of {dt} is wanted")
+        if elevations.numel() != len(self.xs):
+            raise ValueError("one elevation per site")
+        m = qx.numel()
+        if qy.numel() != m or out.numel() != m or found.numel() != m:
+            raise ValueError("qx, qy, out and found differ in size")
+        torch.cuda.current_stream().synchronize()      # inputs written by torch are complete
+        check(lib().fl_interpolate_device(self._h, elevations.data_ptr(), m, qx.data_ptr(),
+                                          qy.data_ptr(), out.data_ptr(), found.data_ptr()))
 
     def interpolate(self, elevations, site):
         v, ok = self.interpolate_many(elevations, np.array([site.x]), np.array([site.y]))
@@ -401,9 +420,10 @@ class Terrain2D:
         """Interpolated elevation at `site` (terrain.rs:35-38), None outside the hull."""
         return self._interpolator().interpolate(self._elev, site)
 
-    def get_elevations(self, xs, ys):
-        """get_elevation for arrays of coordinates at once: NaN where it is None."""
-        return self._interpolator().interpolate_many(self._elev, xs, ys)[0]
+    def get_elevations(self, xs, ys, gpu=False):
+        """get_elevation for arrays of coordinates at once: NaN where it is None
+        (gpu=True: computed on the GPU, the same values)."""
+        return self._interpolator().interpolate_many(self._elev, xs, ys, gpu=gpu)[0]
 
 
 class TerrainGenerator:

@@ -22,9 +22,10 @@ LIB = os.path.join(OUT_DIR, "libfastlem_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_SOURCES = ["solver.cu", "receivers.cu", "basin.cu", "noalloc.cu", "lake_rank.cu",
-                "ordering.cu"]
+                "ordering.cu", "interp_gpu.cu"]
 CXX_SOURCES = ["builder.cpp", "prim_rank.cpp", "server.cpp", "interp.cpp"]
-HEADERS = ["rng.h", "common.cuh", "kernels.h", "fold.cuh", "delaunay.h", "ordering.h"]
+HEADERS = ["rng.h", "common.cuh", "kernels.h", "fold.cuh", "delaunay.h", "ordering.h",
+           "interp.h", "expansion.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xptxas", "-v",

@@ -28,23 +28,11 @@
 
 #include "delaunay.h"
 #include "fastlem_gb300.h"
+#include "interp.h"
 
 namespace fl {
 void set_last_error(const char* msg);
 }
-
-struct fl_interpolator {
-    uint32_t n = 0;
-    std::vector<double> X, Y;
-    std::vector<uint32_t> tri;
-    std::vector<int64_t> half;
-    std::vector<double> ccx, ccy;      // circumcentre of every triangle
-    std::vector<int64_t> vedge;        // a half-edge starting at each vertex (-1: none)
-    // point-location grid: a site near each cell, where walks start
-    double gx0 = 0, gy0 = 0, gsx = 1, gsy = 1;
-    uint32_t gw = 1, gh = 1;
-    std::vector<uint32_t> gsite;
-};
 
 namespace {
 
@@ -250,7 +238,11 @@ int fl_interpolator_create(uint32_t n, const double* xs, const double* ys, fl_in
     return FL_OK;
 }
 
-void fl_interpolator_destroy(fl_interpolator* it) { delete it; }
+void fl_interpolator_destroy(fl_interpolator* it) {
+    if (!it) return;
+    fl::interp_device_release(it->dev);
+    delete it;
+}
 
 int fl_interpolate(const fl_interpolator* it, const double* values, uint64_t count,
                    const double* qx, const double* qy, double* out, uint8_t* found) {

@@ -377,14 +377,29 @@ int64_t fl_triangulate(uint32_t n, const double* xs, const double* ys, uint32_t*
  * interpolation, None outside the sites' convex hull.  fl_interpolate answers `count`
  * queries at once: out[i] = the interpolated value and found[i] = 1, or out[i] = NaN
  * and found[i] = 0 (the reference's None).  A query on a hull edge takes the linear
- * interpolant along it; a query equal to a site returns its value.  Host computation,
- * threads for large batches.
+ * interpolant along it; a query equal to a site returns its value.  fl_interpolate
+ * computes on host threads (large batches in grid-cell order).
  *   fewer than three sites / all collinear / a non-finite site -> FL_ERR_INVALID_ARGUMENT */
 typedef struct fl_interpolator fl_interpolator;
 int fl_interpolator_create(uint32_t n, const double* xs, const double* ys, fl_interpolator** out);
 void fl_interpolator_destroy(fl_interpolator* it);
 int fl_interpolate(const fl_interpolator* it, const double* values, uint64_t count,
                    const double* qx, const double* qy, double* out, uint8_t* found);
+
+/* The same queries on the GPU, with the same results bit for bit: one thread per query
+ * over the triangulation, which is uploaded to the current device on the first call
+ * (later calls use that device).  fl_interpolate_gpu takes host arrays; in
+ * fl_interpolate_device all five arrays are in that device's memory (for instance the
+ * elevations of a solve and a rendering grid made on the device).  Both return when the
+ * results are written.  A query whose natural-neighbour cavity exceeds 2048 triangles
+ * (only with over two thousand sites on one circle) fails the call with
+ * FL_ERR_INVALID_ARGUMENT; the host fl_interpolate has no such limit.
+ *   null interpolator / a null array with count > 0 -> FL_ERR_INVALID_ARGUMENT (before any
+ *   CUDA call); count == 0 -> FL_OK without device work */
+int fl_interpolate_gpu(fl_interpolator* it, const double* values, uint64_t count, const double* qx,
+                       const double* qy, double* out, uint8_t* found);
+int fl_interpolate_device(fl_interpolator* it, const double* values, uint64_t count,
+                          const double* qx, const double* qy, double* out, uint8_t* found);
 
 #ifdef __cplusplus
 }
