@@ -25,7 +25,7 @@ CUDA_SOURCES = ["solver.cu", "receivers.cu", "basin.cu", "noalloc.cu", "lake_ran
                 "ordering.cu", "interp_gpu.cu"]
 CXX_SOURCES = ["builder.cpp", "prim_rank.cpp", "server.cpp", "interp.cpp"]
 HEADERS = ["rng.h", "common.cuh", "kernels.h", "fold.cuh", "delaunay.h", "ordering.h",
-           "interp.h", "expansion.cuh"]
+           "interp.h", "expansion.cuh", "interp_query.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xptxas", "-v",

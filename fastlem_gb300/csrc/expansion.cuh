@@ -12,6 +12,13 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cmath>
+
+// Compiled for the device and, for the host-side probe of the same query code, the host.
+#ifndef FL_HD
+#define FL_HD __host__ __device__
+#endif
+
 namespace fl {
 namespace xp {
 
@@ -20,25 +27,29 @@ constexpr double kEps = 1.1102230246251565e-16;               // 2^-53
 constexpr double kOrientBound = (3.0 + 16.0 * kEps) * kEps;
 constexpr double kIncircleBound = (10.0 + 96.0 * kEps) * kEps;
 
-__device__ __forceinline__ void two_sum(double a, double b, double& x, double& y) {
+FL_HD __forceinline__ void two_sum(double a, double b, double& x, double& y) {
     x = a + b;
     const double bv = x - a;
     const double av = x - bv;
     y = (a - av) + (b - bv);
 }
-__device__ __forceinline__ void two_diff(double a, double b, double& x, double& y) {
+FL_HD __forceinline__ void two_diff(double a, double b, double& x, double& y) {
     x = a - b;
     const double bv = a - x;
     const double av = x + bv;
     y = (a - av) + (bv - b);
 }
-__device__ __forceinline__ void two_prod(double a, double b, double& x, double& y) {
+FL_HD __forceinline__ void two_prod(double a, double b, double& x, double& y) {
     x = a * b;
+#ifdef __CUDA_ARCH__
     y = __fma_rn(a, b, -x);
+#else
+    y = std::fma(a, b, -x);
+#endif
 }
 
 // h <- h + b in place; h holds nh components and has room for nh + 1.
-__device__ inline int grow(double* h, int nh, double b) {
+FL_HD inline int grow(double* h, int nh, double b) {
     double q = b;
     int k = 0;
     for (int i = 0; i < nh; ++i) {
@@ -52,7 +63,7 @@ __device__ inline int grow(double* h, int nh, double b) {
 }
 
 // h <- e * b; h (not e) has room for 2 ne components.
-__device__ inline int scale(const double* e, int ne, double b, double* h) {
+FL_HD inline int scale(const double* e, int ne, double b, double* h) {
     int k = 0;
     double q, hh;
     two_prod(e[0], b, q, hh);
@@ -72,7 +83,7 @@ __device__ inline int scale(const double* e, int ne, double b, double* h) {
 
 // h <- e * f as the sum over f's components of e scaled by each; h has room for
 // 2 ne nf + 1 components, t for 2 ne.
-__device__ inline int mul(const double* e, int ne, const double* f, int nf, double* h, double* t) {
+FL_HD inline int mul(const double* e, int ne, const double* f, int nf, double* h, double* t) {
     int nh = 1;
     h[0] = 0.0;
     for (int j = 0; j < nf; ++j) {
@@ -83,23 +94,23 @@ __device__ inline int mul(const double* e, int ne, const double* f, int nf, doub
 }
 
 // e <- e - f (each of f's components negated and grown in); e has room for ne + nf.
-__device__ inline int sub_into(double* e, int ne, const double* f, int nf) {
+FL_HD inline int sub_into(double* e, int ne, const double* f, int nf) {
     for (int k = 0; k < nf; ++k) ne = grow(e, ne, -f[k]);
     return ne;
 }
-__device__ inline int add_into(double* e, int ne, const double* f, int nf) {
+FL_HD inline int add_into(double* e, int ne, const double* f, int nf) {
     for (int k = 0; k < nf; ++k) ne = grow(e, ne, f[k]);
     return ne;
 }
 
-__device__ __forceinline__ double sign_of(const double* e, int ne) {
+FL_HD __forceinline__ double sign_of(const double* e, int ne) {
     for (int i = ne; i-- > 0;)
         if (e[i] != 0.0) return e[i];
     return 0.0;
 }
 
 // a - b exactly: {roundoff, difference}, or {difference} when the difference is exact.
-__device__ __forceinline__ int diff2(double a, double b, double* h) {
+FL_HD __forceinline__ int diff2(double a, double b, double* h) {
     double x, y;
     two_diff(a, b, x, y);
     if (y != 0.0) {
@@ -118,7 +129,7 @@ constexpr int kAccum = 1952;                        // three such products: <= 1
 constexpr int kScratch = kAccum + kProduct + 40 + 6 * kSmall + 16;
 
 // Sign of (a - c) x (b - c): > 0 counter-clockwise.  xs: kScratch doubles.
-__device__ inline double orient_exact(double ax, double ay, double bx, double by, double cx,
+FL_HD inline double orient_exact(double ax, double ay, double bx, double by, double cx,
                                       double cy, double* xs) {
     double* d = xs;                                 // 4 differences, 2 each
     double* p = xs + 8;                             // kSmall
@@ -134,7 +145,7 @@ __device__ inline double orient_exact(double ax, double ay, double bx, double by
 
 // Sign of the in-circle determinant: > 0 when d is inside the circle through the
 // counter-clockwise a, b, c.  xs: kScratch doubles.
-__device__ inline double incircle_exact(double ax, double ay, double bx, double by, double cx,
+FL_HD inline double incircle_exact(double ax, double ay, double bx, double by, double cx,
                                         double cy, double dx, double dy, double* xs) {
     double* acc = xs;                               // kAccum
     double* prod = acc + kAccum;                    // kProduct

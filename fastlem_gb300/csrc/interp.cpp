@@ -49,14 +49,11 @@ inline void circumcentre(double ax, double ay, double bx, double by, double cx, 
 
 constexpr uint32_t kOutside = UINT32_MAX;
 
-// Triangle holding (x, y) (inside or on its boundary), or kOutside beyond the hull:
-// a visibility walk, which terminates on a Delaunay triangulation with exact
-// orientation tests.
-uint32_t locate(const fl_interpolator& it, double x, double y) {
-    const uint32_t cx = (uint32_t)std::min<double>(it.gw - 1, std::max(0.0, (x - it.gx0) / it.gsx));
-    const uint32_t cy = (uint32_t)std::min<double>(it.gh - 1, std::max(0.0, (y - it.gy0) / it.gsy));
-    const uint32_t site = it.gsite[(uint64_t)cy * it.gw + cx];
-    uint32_t t = (uint32_t)(it.vedge[site] / 3);
+// Walk from triangle t to the triangle holding (x, y) (inside or on its boundary), or
+// kOutside beyond the hull, with *last the triangle the walk stopped in: a visibility
+// walk, the edge tests rotating from edge (step mod 3), which terminates on a Delaunay
+// triangulation with exact orientation tests.
+uint32_t walk(const fl_interpolator& it, uint32_t t, double x, double y, uint32_t* last) {
     const uint64_t limit = 4ull * it.tri.size() + 16;
     for (uint64_t step = 0; step < limit; ++step) {
         bool moved = false;
@@ -64,14 +61,25 @@ uint32_t locate(const fl_interpolator& it, double x, double y) {
             const uint32_t e = 3 * t + (uint32_t)((k + step) % 3);
             const uint32_t a = it.tri[e], b = it.tri[nxt3(e)];
             if (fl::orient2d(it.X[a], it.Y[a], it.X[b], it.Y[b], x, y) < 0.0) {
-                if (it.half[e] < 0) return kOutside;       // beyond a hull edge
+                if (it.half[e] < 0) {                      // beyond a hull edge
+                    *last = t;
+                    return kOutside;
+                }
                 t = (uint32_t)(it.half[e] / 3);
                 moved = true;
             }
         }
-        if (!moved) return t;
+        if (!moved) return *last = t;
     }
+    *last = t;
     return kOutside;
+}
+
+uint32_t locate(const fl_interpolator& it, double x, double y) {
+    const uint32_t cx = (uint32_t)std::min<double>(it.gw - 1, std::max(0.0, (x - it.gx0) / it.gsx));
+    const uint32_t cy = (uint32_t)std::min<double>(it.gh - 1, std::max(0.0, (y - it.gy0) / it.gsy));
+    uint32_t last;
+    return walk(it, it.gtri[(uint64_t)cy * it.gw + cx], x, y, &last);
 }
 
 // Sibson interpolant at (x, y); false outside the hull.
@@ -217,23 +225,52 @@ int fl_interpolator_create(uint32_t n, const double* xs, const double* ys, fl_in
     it->gy0 = y0;
     it->gsx = (x1 > x0 ? (x1 - x0) : 1.0) / g;
     it->gsy = (y1 > y0 ? (y1 - y0) : 1.0) / g;
-    it->gsite.assign((uint64_t)g * g, UINT32_MAX);
+    std::vector<uint32_t> gsite((uint64_t)g * g, UINT32_MAX);
     for (uint32_t v : used) {
         const uint32_t cx = (uint32_t)std::min<double>(g - 1, (it->X[v] - x0) / it->gsx);
         const uint32_t cy = (uint32_t)std::min<double>(g - 1, (it->Y[v] - y0) / it->gsy);
-        it->gsite[(uint64_t)cy * g + cx] = v;
+        gsite[(uint64_t)cy * g + cx] = v;
     }
-    // empty cells take the nearest filled cell before them in row order, else after
-    uint32_t last = UINT32_MAX;
-    for (auto& s : it->gsite) {
-        if (s == UINT32_MAX) s = last;
-        else last = s;
+    // empty cells take the site of a nearest filled cell (breadth-first over the grid from
+    // every filled cell at once, in cell order)
+    std::vector<uint32_t> queue;
+    queue.reserve(gsite.size());
+    for (uint32_t c = 0; c < gsite.size(); ++c)
+        if (gsite[c] != UINT32_MAX) queue.push_back(c);
+    for (size_t h = 0; h < queue.size(); ++h) {
+        const uint32_t c = queue[h], cx = c % g, cy = c / g;
+        const uint32_t nb[4] = {cx > 0 ? c - 1 : UINT32_MAX, cx + 1 < g ? c + 1 : UINT32_MAX,
+                                cy > 0 ? c - g : UINT32_MAX, cy + 1 < g ? c + g : UINT32_MAX};
+        for (uint32_t d : nb)
+            if (d != UINT32_MAX && gsite[d] == UINT32_MAX) {
+                gsite[d] = gsite[c];
+                queue.push_back(d);
+            }
     }
-    last = UINT32_MAX;
-    for (auto s = it->gsite.rbegin(); s != it->gsite.rend(); ++s) {
-        if (*s == UINT32_MAX) *s = last;
-        else last = *s;
+    // each cell's start: walk from a triangle of its site to the cell's centre
+    it->gtri.resize(gsite.size());
+    auto starts = [&](uint64_t a, uint64_t b) {
+        for (uint64_t c = a; c < b; ++c) {
+            const double x = x0 + ((double)(c % g) + 0.5) * it->gsx;
+            const double y = y0 + ((double)(c / g) + 0.5) * it->gsy;
+            walk(*it, (uint32_t)(it->vedge[gsite[c]] / 3), x, y, &it->gtri[c]);
+        }
+    };
+    const uint64_t cells = gsite.size();
+    const unsigned workers =
+        cells < 65536 ? 1u : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    const uint64_t chunk = (cells + workers - 1) / workers;
+    for (unsigned w = 1; w < workers; ++w) {
+        const uint64_t a = std::min<uint64_t>(w * chunk, cells), b = std::min<uint64_t>(a + chunk, cells);
+        try {
+            th.emplace_back(starts, a, b);
+        } catch (const std::system_error&) {
+            starts(a, b);
+        }
     }
+    starts(0, std::min<uint64_t>(chunk, cells));
+    for (auto& t : th) t.join();
     *out = it;
     return FL_OK;
 }

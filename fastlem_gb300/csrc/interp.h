@@ -17,10 +17,11 @@ struct fl_interpolator {
     std::vector<int64_t> half;
     std::vector<double> ccx, ccy;      // circumcentre of every triangle
     std::vector<int64_t> vedge;        // a half-edge starting at each vertex (-1: none)
-    // point-location grid: a site near each cell, where walks start
+    // point-location grid: walks start at the triangle holding the cell's centre (or,
+    // for a centre beyond the hull, the hull triangle the walk to it stopped at)
     double gx0 = 0, gy0 = 0, gsx = 1, gsy = 1;
     uint32_t gw = 1, gh = 1;
-    std::vector<uint32_t> gsite;
+    std::vector<uint32_t> gtri;
     // device queries: the triangulation uploaded on first use, one call at a time
     std::mutex device_mu;
     fl::InterpDevice* dev = nullptr;

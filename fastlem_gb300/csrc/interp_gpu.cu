@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -40,14 +41,14 @@
 #include "expansion.cuh"
 #include "fastlem_gb300.h"
 #include "interp.h"
+#include "interp_query.cuh"
 
 namespace fl {
 void set_last_error(const char* msg);
+using namespace iq;
 
 namespace {
 
-constexpr uint32_t kFastCap = 32;          // pass 1: cavity triangles per query
-constexpr uint64_t kFastWalk = 256;        // pass 1: walk steps per query
 constexpr uint32_t kWideCap = 2048;        // pass 2: cavity triangles per query
 constexpr unsigned kWideBlocks = 32, kWideThreads = 32;
 constexpr uint64_t kChunk = 1ull << 26;    // queries per device round
@@ -57,20 +58,6 @@ constexpr int kThreads = 128;
 // bytes of one pass-2 thread's tables: expansion scratch, cavity, boundary
 constexpr size_t kSlabBytes =
     ((xp::kScratch * sizeof(double) + (2 * kWideCap + 2) * sizeof(uint32_t)) + 255) & ~size_t(255);
-
-enum QueryStatus { kQOutside = 0, kQFound = 1, kQDefer = 2, kQTooLarge = 3 };
-enum StatusWord { kDeferred = 0, kTooLarge = 1, kStatusWords = 2 };
-
-struct View {
-    const double2* __restrict__ xy;
-    const uint32_t* __restrict__ tri;
-    const int32_t* __restrict__ half;
-    const double2* __restrict__ cc;
-    const uint32_t* __restrict__ gtri;
-    double gx0, gy0, gsx, gsy;
-    uint32_t gw, gh;
-    uint64_t walk_limit;                   // the host walk's limit: 4 x half-edges + 16
-};
 
 }  // namespace
 
@@ -96,6 +83,7 @@ struct InterpDevice {
     size_t sort_bytes = 0;
     int* status = nullptr;
     int* h_status = nullptr;
+    uint64_t last_deferred = 0;            // queries of the last call the exact pass answered
     unsigned char* slab = nullptr;
 };
 
@@ -131,189 +119,6 @@ int cuda_fail(const char* what, cudaError_t e) {
         if (e_ != cudaSuccess) return cuda_fail(#call, e_); \
     } while (0)
 
-__device__ __forceinline__ uint32_t nxt3(uint32_t e) { return (e % 3 == 2) ? e - 2 : e + 1; }
-
-// interp.cpp's circumcentre, operation for operation.
-__device__ __forceinline__ double2 circumcentre(double ax, double ay, double bx, double by,
-                                                double cx, double cy) {
-    const double dx = bx - ax, dy = by - ay, ex = cx - ax, ey = cy - ay;
-    const double bl = dx * dx + dy * dy, cl = ex * ex + ey * ey;
-    const double d = 0.5 / (dx * ey - dy * ex);
-    return make_double2(ax + (ey * bl - dy * cl) * d, ay + (dx * cl - ex * bl) * d);
-}
-
-// Circumcentre, relative to q, of the new triangle (a, b, q) on boundary edge e.
-__device__ __forceinline__ double2 new_centre(const View& V, uint32_t e, double x, double y) {
-    const double2 a = V.xy[V.tri[e]], b = V.xy[V.tri[nxt3(e)]];
-    return circumcentre(a.x - x, a.y - y, b.x - x, b.y - y, 0.0, 0.0);
-}
-
-// Sign of orient2d (a, b, q): the filter, then (kExact) the expansions; without them an
-// inconclusive filter sets `defer`.
-template <bool kExact>
-__device__ __forceinline__ double orient(double2 a, double2 b, double x, double y, double* xs,
-                                         bool& defer) {
-    const double l = (a.x - x) * (b.y - y);
-    const double r = (a.y - y) * (b.x - x);
-    const double det = l - r;
-    if (fabs(det) > xp::kOrientBound * (fabs(l) + fabs(r))) return det;
-    if (!kExact) {
-        defer = true;
-        return 0.0;
-    }
-    return xp::orient_exact(a.x, a.y, b.x, b.y, x, y, xs);
-}
-
-template <bool kExact>
-__device__ __forceinline__ double incircle(double2 a, double2 b, double2 c, double x, double y,
-                                           double* xs, bool& defer) {
-    const double adx = a.x - x, ady = a.y - y, bdx = b.x - x, bdy = b.y - y, cdx = c.x - x,
-                 cdy = c.y - y;
-    const double bc = bdx * cdy - cdx * bdy, ca = cdx * ady - adx * cdy, ab = adx * bdy - bdx * ady;
-    const double al = adx * adx + ady * ady, bl = bdx * bdx + bdy * bdy, cl = cdx * cdx + cdy * cdy;
-    const double det = al * bc + bl * ca + cl * ab;
-    const double perm = (fabs(bdx * cdy) + fabs(cdx * bdy)) * al +
-                        (fabs(cdx * ady) + fabs(adx * cdy)) * bl +
-                        (fabs(adx * bdy) + fabs(bdx * ady)) * cl;
-    if (fabs(det) > xp::kIncircleBound * perm) return det;
-    if (!kExact) {
-        defer = true;
-        return 0.0;
-    }
-    return xp::incircle_exact(a.x, a.y, b.x, b.y, c.x, c.y, x, y, xs);
-}
-
-__device__ __forceinline__ bool holds(const uint32_t* s, uint32_t n, uint32_t t) {
-    for (uint32_t i = 0; i < n; ++i)
-        if (s[i] == t) return true;
-    return false;
-}
-
-// Grid cell coordinate of q, clamped as interp.cpp's locate clamps it.
-__device__ __forceinline__ uint32_t cell_coord(double q, double q0, double step, uint32_t cells) {
-    double f = (q - q0) / step;
-    f = (0.0 < f) ? f : 0.0;
-    const double hi = (double)(cells - 1);
-    f = (f < hi) ? f : hi;
-    return (uint32_t)f;
-}
-
-// One query: the status and, when found, the value.  cav holds cap triangles, bnd
-// cap + 2 edges; xs is the exact stages' scratch (kExact only).
-template <bool kExact>
-__device__ int query(const View& V, const double* __restrict__ f, double x, double y,
-                     uint32_t* cav, uint32_t* bnd, uint32_t cap, double* xs, double& out) {
-    if (!isfinite(x) || !isfinite(y)) return kQOutside;
-    bool defer = false;
-    const uint32_t cx = cell_coord(x, V.gx0, V.gsx, V.gw);
-    const uint32_t cy = cell_coord(y, V.gy0, V.gsy, V.gh);
-    uint32_t t = V.gtri[(uint64_t)cy * V.gw + cx];
-    const uint64_t limit = kExact ? V.walk_limit : kFastWalk;
-    uint64_t step = 0;
-    uint32_t rot = 0;                                     // step mod 3
-    for (; step < limit; ++step) {
-        bool moved = false;
-        for (uint32_t k = 0; k < 3 && !moved; ++k) {
-            const uint32_t e = 3 * t + (k + rot) % 3;
-            const double s = orient<kExact>(V.xy[V.tri[e]], V.xy[V.tri[nxt3(e)]], x, y, xs, defer);
-            if (defer) return kQDefer;
-            if (s < 0.0) {
-                const int32_t o = V.half[e];
-                if (o < 0) return kQOutside;              // beyond a hull edge
-                t = (uint32_t)o / 3;
-                moved = true;
-            }
-        }
-        if (!moved) break;
-        rot = rot == 2 ? 0 : rot + 1;
-    }
-    if (step == limit) return kExact ? kQOutside : kQDefer;
-    for (uint32_t k = 0; k < 3; ++k) {
-        const uint32_t v = V.tri[3 * t + k];
-        const double2 p = V.xy[v];
-        if (p.x == x && p.y == y) {
-            out = f[v];
-            return kQFound;
-        }
-    }
-    // the cavity
-    uint32_t nc = 1;
-    cav[0] = t;
-    for (uint32_t i = 0; i < nc; ++i) {
-        const uint32_t ti = cav[i];
-        for (uint32_t k = 0; k < 3; ++k) {
-            const int32_t o = V.half[3 * ti + k];
-            if (o < 0) continue;
-            const uint32_t u = (uint32_t)o / 3;
-            if (holds(cav, nc, u)) continue;
-            const double s = incircle<kExact>(V.xy[V.tri[3 * u]], V.xy[V.tri[3 * u + 1]],
-                                              V.xy[V.tri[3 * u + 2]], x, y, xs, defer);
-            if (defer) return kQDefer;
-            if (s > 0.0) {
-                if (nc == cap) return kExact ? kQTooLarge : kQDefer;
-                cav[nc++] = u;
-            }
-        }
-    }
-    // boundary edges a -> b, counter-clockwise around q
-    uint32_t nb = 0;
-    for (uint32_t i = 0; i < nc; ++i)
-        for (uint32_t k = 0; k < 3; ++k) {
-            const uint32_t e = 3 * cav[i] + k;
-            const int32_t o = V.half[e];
-            if (o >= 0 && holds(cav, nc, (uint32_t)o / 3)) continue;
-            const uint32_t a = V.tri[e], b = V.tri[nxt3(e)];
-            if (o < 0) {
-                const double2 pa = V.xy[a], pb = V.xy[b];
-                const double s = orient<kExact>(pa, pb, x, y, xs, defer);
-                if (defer) return kQDefer;
-                if (s == 0.0) {                           // on a hull edge: linear along it
-                    const double dx = pb.x - pa.x, dy = pb.y - pa.y;
-                    const double w = ((x - pa.x) * dx + (y - pa.y) * dy) / (dx * dx + dy * dy);
-                    out = f[a] + w * (f[b] - f[a]);
-                    return kQFound;
-                }
-            }
-            if (nb == cap + 2) return kExact ? kQTooLarge : kQDefer;
-            bnd[nb++] = e;
-        }
-    double num = 0.0, den = 0.0;
-    for (uint32_t o = 0; o < nb; ++o) {                   // o: the edge leaving v
-        const uint32_t eo = bnd[o];
-        const uint32_t v = V.tri[eo];
-        uint32_t i = nb;                                  // the edge arriving at v
-        for (uint32_t j = 0; j < nb; ++j)
-            if (V.tri[nxt3(bnd[j])] == v) {
-                i = j;
-                break;
-            }
-        if (i == nb) return kQOutside;
-        const double2 first = new_centre(V, bnd[i], x, y);
-        double2 prev = first;
-        double area2 = 0.0;                               // shoelace, closed polygon
-        uint32_t h = nxt3(bnd[i]);
-        for (uint32_t guard = 0;; ++guard) {
-            const double2 c = V.cc[h / 3];
-            const double2 p = make_double2(c.x - x, c.y - y);
-            area2 += prev.x * p.y - p.x * prev.y;
-            prev = p;
-            if (h == eo) break;
-            const int32_t tw = V.half[h];
-            if (tw < 0 || guard > nc || !holds(cav, nc, (uint32_t)tw / 3)) return kQOutside;
-            h = nxt3((uint32_t)tw);
-        }
-        const double2 last = new_centre(V, eo, x, y);
-        area2 += prev.x * last.y - last.x * prev.y;
-        area2 += last.x * first.y - first.x * last.y;
-        const double w = fabs(area2);
-        num += w * f[v];
-        den += w;
-    }
-    if (!(den > 0.0)) return kQOutside;
-    out = num / den;
-    return kQFound;
-}
-
 // Grid cell of every query (non-finite coordinates: cell 0) and the identity order.
 __global__ void k_cell_keys(View V, uint64_t count, const double* __restrict__ qx,
                             const double* __restrict__ qy, uint32_t* __restrict__ keys,
@@ -341,8 +146,9 @@ __global__ void __launch_bounds__(kThreads) k_interp_fast(View V, const double* 
     if (k >= count) return;
     const uint32_t i = order ? order[k] : (uint32_t)k;
     uint32_t cav[kFastCap], bnd[kFastCap + 2];
+    double2 centre[kFastCap + 2];
     double v = 0.0;
-    const int s = query<false>(V, f, qx[i], qy[i], cav, bnd, kFastCap, nullptr, v);
+    const int s = query_fast(V, f, qx[i], qy[i], cav, bnd, centre, v);
     if (s == kQDefer) {
         deferred[atomicAdd(&status[kDeferred], 1)] = i;
         return;
@@ -366,6 +172,7 @@ __global__ void __launch_bounds__(kWideThreads) k_interp_exact(View V, const dou
     uint32_t* cav = reinterpret_cast<uint32_t*>(mine + xp::kScratch * sizeof(double));
     uint32_t* bnd = cav + kWideCap;
     const uint32_t nd = (uint32_t)status[kDeferred];
+    if (w == 0) atomicAdd(reinterpret_cast<unsigned long long*>(status + kDeferredTotal), nd);
     for (uint32_t k = w; k < nd; k += gridDim.x * blockDim.x) {
         const uint32_t i = deferred[k];
         double v = 0.0;
@@ -409,14 +216,13 @@ int ensure_device(fl_interpolator* it) {
     for (uint64_t t = 0; t < tris; ++t) cc[t] = make_double2(it->ccx[t], it->ccy[t]);
     std::vector<int32_t> half(halves);
     for (uint64_t h = 0; h < halves; ++h) half[h] = (int32_t)it->half[h];
-    std::vector<uint32_t> gtri(it->gsite.size());
-    for (size_t c = 0; c < gtri.size(); ++c) gtri[c] = (uint32_t)(it->vedge[it->gsite[c]] / 3);
+    const std::vector<uint32_t>& gtri = it->gtri;
     struct Up { void** dst; const void* src; size_t bytes; } ups[] = {
         {(void**)&d->xy, xy.data(), xy.size() * sizeof(double2)},
         {(void**)&d->tri, it->tri.data(), halves * sizeof(uint32_t)},
         {(void**)&d->half, half.data(), halves * sizeof(int32_t)},
         {(void**)&d->cc, cc.data(), cc.size() * sizeof(double2)},
-        {(void**)&d->gtri, gtri.data(), gtri.size() * sizeof(uint32_t)},
+        {(void**)&d->gtri, (const void*)gtri.data(), gtri.size() * sizeof(uint32_t)},
     };
     for (auto& u : ups) {
         if ((e = cudaMalloc(u.dst, std::max<size_t>(16, u.bytes))) != cudaSuccess)
@@ -502,6 +308,9 @@ int finish(InterpDevice* d, const char* who) {
     IG_CU(cudaMemcpyAsync(d->h_status, d->status, kStatusWords * sizeof(int), cudaMemcpyDeviceToHost,
                           d->stream));
     IG_CU(cudaStreamSynchronize(d->stream));
+    uint64_t total;
+    std::memcpy(&total, d->h_status + kDeferredTotal, 8);
+    d->last_deferred = total;
     if (d->h_status[kTooLarge]) {
         std::string m = std::string(who) +
                         ": a query's natural-neighbour cavity exceeds 2048 triangles (sites on one circle)";
@@ -566,6 +375,44 @@ int fl_interpolate_device(fl_interpolator* it, const double* values, uint64_t co
         if (int rc = run_round(d, values, m, qx + a, qy + a, out + a, found + a)) return rc;
     }
     return finish(d, "fl_interpolate_device");
+}
+
+uint64_t fl_interpolator_last_deferred(const fl_interpolator* it) {
+    return it && it->dev ? it->dev->last_deferred : 0;
+}
+
+// The device query code compiled for the host, one query after another: exact = 0 runs
+// the first pass (status 2: deferred), exact = 1 the second (status 3: cavity too large).
+int fl_probe_interp_query(const fl_interpolator* it, const double* values, uint64_t count,
+                          const double* qx, const double* qy, int exact, double* out,
+                          int32_t* status) {
+    using namespace fl;
+    if (!it || (count && (!values || !qx || !qy || !out || !status))) {
+        set_last_error("fl_probe_interp_query: null argument");
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    const uint64_t halves = it->tri.size();
+    std::vector<double2> xy(it->n), cc(halves / 3);
+    for (uint32_t v = 0; v < it->n; ++v) xy[v] = make_double2(it->X[v], it->Y[v]);
+    for (uint64_t t = 0; t < halves / 3; ++t) cc[t] = make_double2(it->ccx[t], it->ccy[t]);
+    std::vector<int32_t> half(halves);
+    for (uint64_t h = 0; h < halves; ++h) half[h] = (int32_t)it->half[h];
+    const std::vector<uint32_t>& gtri = it->gtri;
+    const View V{xy.data(), it->tri.data(), half.data(), cc.data(), gtri.data(), it->gx0, it->gy0,
+                 it->gsx, it->gsy, it->gw, it->gh, 4ull * halves + 16};
+    std::vector<double> xs(xp::kScratch);
+    std::vector<uint32_t> cav(kWideCap), bnd(kWideCap + 2);
+    std::vector<double2> centre(kFastCap + 2);
+    for (uint64_t i = 0; i < count; ++i) {
+        double v = NAN;
+        const int s = exact ? query<true>(V, values, qx[i], qy[i], cav.data(), bnd.data(), kWideCap,
+                                          xs.data(), v)
+                            : query_fast(V, values, qx[i], qy[i], cav.data(), bnd.data(),
+                                         centre.data(), v);
+        out[i] = s == kQFound ? v : NAN;
+        status[i] = s;
+    }
+    return FL_OK;
 }
 
 }  // extern "C"

@@ -400,6 +400,16 @@ int fl_interpolate_gpu(fl_interpolator* it, const double* values, uint64_t count
                        const double* qy, double* out, uint8_t* found);
 int fl_interpolate_device(fl_interpolator* it, const double* values, uint64_t count,
                           const double* qx, const double* qy, double* out, uint8_t* found);
+/* Queries of the last GPU call whose first pass could not decide them (a predicate
+ * filter inconclusive, a cavity over 32 triangles or a walk over 256 steps), answered by
+ * the exact second pass. */
+uint64_t fl_interpolator_last_deferred(const fl_interpolator* it);
+/* Probe: the GPU natural-neighbour query code compiled for the host, one query at a time:
+ * exact = 0 is the device's first pass (status 2: deferred to the second), exact = 1 the
+ * second (status 3: cavity over 2048 triangles); status 0 outside, 1 found. */
+int fl_probe_interp_query(const fl_interpolator* it, const double* values, uint64_t count,
+                          const double* qx, const double* qy, int exact, double* out,
+                          int32_t* status);
 
 #ifdef __cplusplus
 }
