@@ -42,7 +42,7 @@ EXPORTS = [
     "fl_probe_rng_f64", "fl_probe_chain_fold", "fl_random_sites", "fl_relax_sites", "fl_build_graph", "fl_triangulate",
     "fl_interpolator_create", "fl_interpolator_destroy", "fl_interpolate", "fl_lake_rank",
     "fl_interpolate_gpu", "fl_interpolate_device", "fl_interpolator_last_deferred",
-    "fl_probe_interp_query",
+    "fl_probe_interp_query", "fl_probe_prefilters",
 ]
 
 c_u32, c_u64, c_int, c_dbl, vp = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
@@ -89,6 +89,7 @@ def lib():
     L.fl_interpolator_last_deferred.argtypes = [vp]
     L.fl_interpolator_last_deferred.restype = c_u64
     L.fl_probe_interp_query.argtypes = [vp, vp, c_u64, vp, vp, c_int, vp, vp]
+    L.fl_probe_prefilters.argtypes = [c_u64, vp, vp]
     L.fl_lake_rank.argtypes = [c_u32, vp, vp, vp, vp, c_u32, vp]
     L.fl_server_create.argtypes = [c_u64, c_u32, P(vp)]
     L.fl_server_add_model.argtypes = [vp, c_u32, vp, vp, vp, vp, vp, c_u32, vp, vp, P(c_u32)]

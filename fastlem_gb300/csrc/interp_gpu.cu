@@ -65,6 +65,7 @@ struct InterpDevice {
     int device = 0;
     cudaStream_t stream = nullptr;
     double2* xy = nullptr;
+    float2* xyf = nullptr;
     uint32_t* tri = nullptr;
     int32_t* half = nullptr;
     double2* cc = nullptr;
@@ -93,7 +94,7 @@ void interp_device_release(InterpDevice* d) {
     cudaGetDevice(&cur);
     cudaSetDevice(d->device);
     if (d->stream) cudaStreamSynchronize(d->stream);
-    void* ptrs[] = {d->xy,   d->tri,      d->half,     d->cc,  d->gtri,    d->values, d->qx,
+    void* ptrs[] = {d->xy,   d->xyf,  d->tri,      d->half,     d->cc,  d->gtri,    d->values, d->qx,
                     d->qy,   d->out,      d->found,    d->keys, d->keys_alt, d->idx,  d->idx_alt,
                     d->deferred, d->sort_tmp, d->status, d->slab};
     for (void* p : ptrs)
@@ -142,13 +143,16 @@ __global__ void __launch_bounds__(kThreads) k_interp_fast(View V, const double* 
                                                           uint8_t* __restrict__ found,
                                                           uint32_t* __restrict__ deferred,
                                                           int* __restrict__ status) {
+    // every thread of a warp takes part in the warp-synchronous query, with or without one
     const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    const uint32_t i = order ? order[k] : (uint32_t)k;
+    const bool active = k < count;
+    const uint32_t i = !active ? 0u : order ? order[k] : (uint32_t)k;
     uint32_t cav[kFastCap], bnd[kFastCap + 2];
     double2 centre[kFastCap + 2];
     double v = 0.0;
-    const int s = query_fast(V, f, qx[i], qy[i], cav, bnd, centre, v);
+    const int s = query_fast(V, f, active, active ? qx[i] : 0.0, active ? qy[i] : 0.0, cav, bnd,
+                             centre, v);
+    if (!active) return;
     if (s == kQDefer) {
         deferred[atomicAdd(&status[kDeferred], 1)] = i;
         return;
@@ -212,13 +216,20 @@ int ensure_device(fl_interpolator* it) {
     if ((e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking)) != cudaSuccess)
         return fail(cuda_fail("cudaStreamCreate", e));
     std::vector<double2> xy(it->n), cc(tris);
-    for (uint32_t v = 0; v < it->n; ++v) xy[v] = make_double2(it->X[v], it->Y[v]);
+    std::vector<float2> xyf(it->n);
+    float smax = 0.0f;
+    for (uint32_t v = 0; v < it->n; ++v) {
+        xy[v] = make_double2(it->X[v], it->Y[v]);
+        xyf[v] = make_float2((float)it->X[v], (float)it->Y[v]);
+        smax = std::max(smax, std::max(std::fabs(xyf[v].x), std::fabs(xyf[v].y)));
+    }
     for (uint64_t t = 0; t < tris; ++t) cc[t] = make_double2(it->ccx[t], it->ccy[t]);
     std::vector<int32_t> half(halves);
     for (uint64_t h = 0; h < halves; ++h) half[h] = (int32_t)it->half[h];
     const std::vector<uint32_t>& gtri = it->gtri;
     struct Up { void** dst; const void* src; size_t bytes; } ups[] = {
         {(void**)&d->xy, xy.data(), xy.size() * sizeof(double2)},
+        {(void**)&d->xyf, xyf.data(), xyf.size() * sizeof(float2)},
         {(void**)&d->tri, it->tri.data(), halves * sizeof(uint32_t)},
         {(void**)&d->half, half.data(), halves * sizeof(int32_t)},
         {(void**)&d->cc, cc.data(), cc.size() * sizeof(double2)},
@@ -236,7 +247,7 @@ int ensure_device(fl_interpolator* it) {
         (e = cudaMalloc((void**)&d->slab, (size_t)kWideBlocks * kWideThreads * kSlabBytes)) != cudaSuccess)
         return fail(cuda_fail("cudaMalloc", e));
     d->view = View{d->xy, d->tri, d->half, d->cc, d->gtri, it->gx0, it->gy0, it->gsx, it->gsy,
-                   it->gw, it->gh, 4ull * halves + 16};
+                   it->gw, it->gh, 4ull * halves + 16, d->xyf, smax};
     it->dev = d;
     return FL_OK;
 }
@@ -377,6 +388,37 @@ int fl_interpolate_device(fl_interpolator* it, const double* values, uint64_t co
     return finish(d, "fl_interpolate_device");
 }
 
+// Probe of the float prefilters: per case (ax, ay, bx, by, cx, cy, qx, qy), the
+// prefilter's orientation sign of (a, b, q) and in-circle sign of (a, b, c, q) (0:
+// undecided) and the exact signs, in out[4 i .. 4 i + 3].
+int fl_probe_prefilters(uint64_t count, const double* cases, int32_t* out) {
+    using namespace fl;
+    if (count && (!cases || !out)) {
+        set_last_error("fl_probe_prefilters: null argument");
+        return FL_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<double> xs(xp::kScratch);
+    for (uint64_t i = 0; i < count; ++i) {
+        const double* c = cases + 8 * i;
+        float smax = 0.0f;
+        float2 f[3];
+        for (int k = 0; k < 3; ++k) {
+            f[k] = make_float2((float)c[2 * k], (float)c[2 * k + 1]);
+            smax = std::max(smax, std::max(std::fabs(f[k].x), std::fabs(f[k].y)));
+        }
+        View V{};
+        V.smax = smax;
+        const QueryF q = query_f(V, c[6], c[7]);
+        auto sgn = [](double v) { return v > 0.0 ? 1 : (v < 0.0 ? -1 : 0); };
+        out[4 * i] = q.ok ? orient_f(f[0], f[1], q) : 0;
+        out[4 * i + 1] = q.ok ? incircle_f(f[0], f[1], f[2], q) : 0;
+        out[4 * i + 2] = sgn(xp::orient_exact(c[0], c[1], c[2], c[3], c[6], c[7], xs.data()));
+        out[4 * i + 3] =
+            sgn(xp::incircle_exact(c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7], xs.data()));
+    }
+    return FL_OK;
+}
+
 uint64_t fl_interpolator_last_deferred(const fl_interpolator* it) {
     return it && it->dev ? it->dev->last_deferred : 0;
 }
@@ -393,13 +435,20 @@ int fl_probe_interp_query(const fl_interpolator* it, const double* values, uint6
     }
     const uint64_t halves = it->tri.size();
     std::vector<double2> xy(it->n), cc(halves / 3);
-    for (uint32_t v = 0; v < it->n; ++v) xy[v] = make_double2(it->X[v], it->Y[v]);
+    std::vector<float2> xyf(it->n);
+    float smax = 0.0f;
+    for (uint32_t v = 0; v < it->n; ++v) {
+        xy[v] = make_double2(it->X[v], it->Y[v]);
+        xyf[v] = make_float2((float)it->X[v], (float)it->Y[v]);
+        smax = std::max(smax, std::max(std::fabs(xyf[v].x), std::fabs(xyf[v].y)));
+    }
     for (uint64_t t = 0; t < halves / 3; ++t) cc[t] = make_double2(it->ccx[t], it->ccy[t]);
     std::vector<int32_t> half(halves);
     for (uint64_t h = 0; h < halves; ++h) half[h] = (int32_t)it->half[h];
     const std::vector<uint32_t>& gtri = it->gtri;
-    const View V{xy.data(), it->tri.data(), half.data(), cc.data(), gtri.data(), it->gx0, it->gy0,
-                 it->gsx, it->gsy, it->gw, it->gh, 4ull * halves + 16};
+    const View V{xy.data(),  it->tri.data(), half.data(), cc.data(), gtri.data(),
+                 it->gx0,    it->gy0,        it->gsx,     it->gsy,   it->gw,
+                 it->gh,     4ull * halves + 16, xyf.data(), smax};
     std::vector<double> xs(xp::kScratch);
     std::vector<uint32_t> cav(kWideCap), bnd(kWideCap + 2);
     std::vector<double2> centre(kFastCap + 2);
@@ -407,7 +456,7 @@ int fl_probe_interp_query(const fl_interpolator* it, const double* values, uint6
         double v = NAN;
         const int s = exact ? query<true>(V, values, qx[i], qy[i], cav.data(), bnd.data(), kWideCap,
                                           xs.data(), v)
-                            : query_fast(V, values, qx[i], qy[i], cav.data(), bnd.data(),
+                            : query_fast(V, values, true, qx[i], qy[i], cav.data(), bnd.data(),
                                          centre.data(), v);
         out[i] = s == kQFound ? v : NAN;
         status[i] = s;

@@ -404,6 +404,11 @@ int fl_interpolate_device(fl_interpolator* it, const double* values, uint64_t co
  * filter inconclusive, a cavity over 32 triangles or a walk over 256 steps), answered by
  * the exact second pass. */
 uint64_t fl_interpolator_last_deferred(const fl_interpolator* it);
+/* Probe of the GPU queries' single-precision prefilters on count cases of 8 doubles
+ * (a, b, c, q): out[4 i + 0, 1] the prefilter's orientation sign of (a, b, q) and
+ * in-circle sign of (a, b, c, q), 0 where it leaves the case to double precision;
+ * out[4 i + 2, 3] the exact signs. */
+int fl_probe_prefilters(uint64_t count, const double* cases, int32_t* out);
 /* Probe: the GPU natural-neighbour query code compiled for the host, one query at a time:
  * exact = 0 is the device's first pass (status 2: deferred to the second), exact = 1 the
  * second (status 3: cavity over 2048 triangles); status 0 outside, 1 found. */
