@@ -741,9 +741,9 @@ def bench_interp(args, d, emit=True):
         v, ok = it.interpolate_many(elev, hx, hy, gpu=True)
     e2e_s = (time.perf_counter() - t) / steps
     dev_vals = out.cpu().numpy()
-    # host baseline on a band of rows (about 10 s of host work at most)
-    rows = max(1, min(g, int(2_000_000 // g)))
-    band = slice((g // 2) * g, (g // 2 + rows) * g)
+    # host baseline on a band of rows (8M queries: about a second on 16 host threads)
+    rows = max(1, min(g, int(8_000_000 // g)))
+    band = slice(((g - rows) // 2) * g, ((g - rows) // 2 + rows) * g)
     it.interpolate_many(elev, qx[:1000], qy[:1000])
     t = time.perf_counter()
     hv, hok = it.interpolate_many(elev, qx[band], qy[band])
