@@ -209,7 +209,7 @@ def kernel_stats(handle):
     return out
 
 
-TUNING = ("low_ilp", "walk_per_sm", "sized_grids", "gpu_rank", "kahn_min_width")
+TUNING = ("low_ilp", "walk_per_sm", "sized_grids", "gpu_rank", "kahn_min_width", "kahn_ilp")
 
 
 def set_tuning(**kw):
