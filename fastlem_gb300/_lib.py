@@ -209,7 +209,7 @@ def kernel_stats(handle):
     return out
 
 
-TUNING = ("low_ilp", "walk_per_sm", "sized_grids", "gpu_rank", "kahn_min_width", "kahn_ilp")
+TUNING = ("low_ilp", "walk_per_sm", "sized_grids", "gpu_rank", "kahn_min_width")
 
 
 def set_tuning(**kw):

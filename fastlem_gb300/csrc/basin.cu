@@ -114,77 +114,9 @@ __global__ void k_collect_leaves(uint32_t n, const uint32_t* __restrict__ pendin
         [&](uint32_t v, uint32_t pos) { order[pos] = v; });
 }
 
-// The drainage areas of K sites with all their loads in flight together: for rows of
-// up to kRowIlp slots the columns, then the receivers, then the donor areas of all K
-// sites are loaded a phase at a time (three memory latencies for the K sites); longer
-// rows (rare) take a plain loop.  Each site's sum is pull_area's: the cell area, then
-// the donors in reverse adjacency order.  K = 1 is pull_area itself.
-constexpr int kRowIlp = 8;
-template <int K>
-__device__ __forceinline__ void pull_areas(const uint32_t (&v)[K], double (&a)[K],
-                                           const uint32_t* __restrict__ row,
-                                           const uint32_t* __restrict__ col,
-                                           const uint32_t* __restrict__ next,
-                                           const double* __restrict__ area, const double* A) {
-    if (K == 1) {
-        if (v[0] != kNone) a[0] = pull_area(v[0], row, col, next, area, A);
-        return;
-    }
-    uint32_t s0[K], deg[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        deg[k] = 0;
-        s0[k] = 0;
-        if (v[k] != kNone) {
-            s0[k] = row[v[k]];
-            deg[k] = row[v[k] + 1] - s0[k];
-            a[k] = area[v[k]];
-        }
-    }
-    uint32_t d[K][kRowIlp];
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-#pragma unroll
-        for (int j = 0; j < kRowIlp; ++j)
-            if ((uint32_t)j < deg[k] && deg[k] <= (uint32_t)kRowIlp) d[k][j] = col[s0[k] + j];
-    uint32_t don[K];                                   // donor slots, one bit each
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        don[k] = 0;
-#pragma unroll
-        for (int j = 0; j < kRowIlp; ++j)
-            if ((uint32_t)j < deg[k] && deg[k] <= (uint32_t)kRowIlp && d[k][j] != v[k] &&
-                next[d[k][j]] == v[k])
-                don[k] |= 1u << j;
-    }
-    double val[K][kRowIlp];
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-#pragma unroll
-        for (int j = 0; j < kRowIlp; ++j)
-            if (don[k] >> j & 1u) val[k][j] = __ldcg(&A[d[k][j]]);
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if (v[k] == kNone) continue;
-        if (deg[k] <= (uint32_t)kRowIlp) {
-#pragma unroll
-            for (int j = kRowIlp - 1; j >= 0; --j)
-                if (don[k] >> j & 1u) a[k] = __dadd_rn(a[k], val[k][j]);
-        } else {
-            for (uint32_t sl = s0[k] + deg[k]; sl-- > s0[k];) {
-                const uint32_t dd = col[sl];
-                if (dd != v[k] && next[dd] == v[k]) a[k] = __dadd_rn(a[k], __ldcg(&A[dd]));
-            }
-        }
-    }
-}
-
 // Kahn rounds.  order[0, nleaves) holds the leaves; rounds append the next frontier
 // after the current one.  Writes hgt (round) and A of processed sites, the round
-// offsets roff[0..r_stop+1] and meta[kMetaRStop] = r_stop.  Each thread takes K sites
-// of a round at a time, their loads in flight together; the frontier's order within a
-// round follows the appends and changes nothing but memory order.
-template <int K>
+// offsets roff[0..r_stop+1] and meta[kMetaRStop] = r_stop.
 __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
                        const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
                        const double* __restrict__ area, double* A, uint32_t* pending,
@@ -206,43 +138,23 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
         uint32_t* cnt = &meta[kMetaCnt0 + (r % 3)];
         if (gtid == 0) meta[kMetaCnt0 + ((r + 1) % 3)] = 0;
         // block-uniform trip count: block_append synchronises the block
-        for (uint32_t tile = beg + blockIdx.x * blockDim.x * K; tile < end; tile += stride * K) {
-            uint32_t v[K];
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const uint32_t idx = tile + (uint32_t)k * blockDim.x + threadIdx.x;
-                v[k] = idx < end ? __ldcg(&order[idx]) : kNone;
+        for (uint32_t tile = beg + blockIdx.x * blockDim.x; tile < end; tile += stride) {
+            const uint32_t idx = tile + threadIdx.x;
+            bool ready = false;
+            uint32_t p = 0;
+            if (idx < end) {
+                uint32_t v = __ldcg(&order[idx]);
+                // round 0 is the leaves: no donors, the drainage area is the cell area
+                A[v] = (r == 0) ? area[v] : pull_area(v, row, col, next, area, A);
+                hgt[v] = r;
+                p = next[v];
+                ready = p != v && atomicSub(&pending[p], 1u) == 1u;
             }
-            double a[K];
-            if (r == 0) {                 // round 0 is the leaves: the drainage area is the cell area
-#pragma unroll
-                for (int k = 0; k < K; ++k)
-                    if (v[k] != kNone) a[k] = area[v[k]];
-            } else {
-                pull_areas<K>(v, a, row, col, next, area, A);
-            }
-            uint32_t p[K];
-            bool ready[K];
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                p[k] = 0;
-                if (v[k] != kNone) {
-                    A[v[k]] = a[k];
-                    hgt[v[k]] = r;
-                    p[k] = next[v[k]];
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < K; ++k)
-                ready[k] = v[k] != kNone && p[k] != v[k] && atomicSub(&pending[p[k]], 1u) == 1u;
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                uint32_t pos = block_append(cnt, ready[k]);
-                if (pos != kNone) {
-                    pos += end;
-                    if (pos < n) order[pos] = p[k];
-                    else set_error(flags, kErrForest);
-                }
+            uint32_t pos = block_append(cnt, ready);
+            if (pos != kNone) {
+                pos += end;
+                if (pos < n) order[pos] = p;
+                else set_error(flags, kErrForest);
             }
         }
         if (!grid_barrier(flags)) return;
@@ -1614,8 +1526,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     const uint32_t n = a.n;
     const unsigned nb = (n + kThreads - 1) / kThreads;
     const bool sz = a.sized_grids;
-    const void* kahn = a.kahn_ilp >= 2 ? (const void*)k_kahn<2> : (const void*)k_kahn<1>;
-    const unsigned g_kahn = sized_grid(sz, coop_grid(kahn, kThreads, 8), n, kThreads * 8);
+    const unsigned g_kahn = sized_grid(sz, coop_grid((const void*)k_kahn, kThreads, 8), n, kThreads * 8);
     const unsigned g_rank = sized_grid(sz, coop_grid((const void*)k_s_rank, kRoundBlock, 2), n / 8,
                                        kRoundBlock * 4);
     // ordered compactions: one block range each, two blocks per SM
@@ -1640,9 +1551,9 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     // Kahn rounds: order 4 + next 4 + row 8 + area 8 + A 8 + hgt 4 + pending 4 per site,
     // col 4 + next 4 per slot, donor areas 8 per site
     hk.begin(hk.ctx);
-    e = coop_launch_ptr(kahn, g_kahn, kThreads, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
-                        a.hgt, a.order, a.roff, a.rtime, a.max_rounds, a.kahn_min_width, a.meta,
-                        a.flags);
+    e = coop_launch(k_kahn, g_kahn, kThreads, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
+                    a.hgt, a.order, a.roff, a.rtime, a.max_rounds, a.kahn_min_width, a.meta,
+                    a.flags);
     hk.end(hk.ctx, kcKahn, 48.0 * n + 8.0 * nnz);
     if (e != cudaSuccess) return e;
 

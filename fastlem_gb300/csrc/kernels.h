@@ -48,7 +48,6 @@ const std::vector<ScheduleEntry>& schedule();
 // fl_set_tuning at run time.
 struct Tuning {
     int low_ilp = -1;
-    int kahn_ilp = -1;            // bottom-up Kahn rounds: sites in flight per thread (1, 2)
     int walk_per_sm = -1;
     int64_t kahn_min_width = -1;
     int sized_grids = -1;
@@ -193,7 +192,6 @@ struct BasinArgs {
     uint32_t* corder_up;    // chains by height, lowest first: the bottom-up claim order
     uint32_t walk_grid;     // blocks of the persistent chain walkers (all co-resident)
     int low_ilp;            // top-down Kahn rounds: sites in flight per thread
-    int kahn_ilp;           // bottom-up Kahn rounds: sites in flight per thread
     bool sized_grids;       // cooperative grids scaled to n (else the whole GPU)
     double* el;             // skeleton elevations in layout order (slope limits only)
     uint32_t* cbas;         // per chain: basin outlet, its response time and elevation

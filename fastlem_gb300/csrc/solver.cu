@@ -67,9 +67,6 @@ constexpr uint32_t kKahnMinWidthEarly = 8192;
 constexpr uint32_t kEarlyPasses = 2;
 
 // The stop width for a model of n sites (packed: several terrains).
-// Bottom-up Kahn rounds: sites in flight per thread unless tuned otherwise.
-constexpr int kKahnIlp = 1;
-
 uint32_t kahn_min_width(uint32_t n, bool packed = false) {
     const uint32_t w = fl::shape_for(n, packed).kahn_min_width;
     if (w) return w;
@@ -339,7 +336,6 @@ Tuning& tuning() {
         };
         const long ilp = env("FL_LOW_ILP", 1, 4, -1);
         d.low_ilp = ilp < 0 ? -1 : ilp >= 4 ? 4 : ilp >= 2 ? 2 : 1;
-        d.kahn_ilp = (int)env("FL_KAHN_ILP", 1, 2, -1);
         d.walk_per_sm = (int)env("FL_WALK_PER_SM", 0, 64, -1);
         d.kahn_min_width = env("FL_KAHN_MIN_WIDTH", 256, 1l << 24, -1);
         d.gpu_rank = env("FL_GPU_RANK", 0, 1, 1) != 0;
@@ -1263,7 +1259,6 @@ int enqueue_basin_pass(fl_graph* g, bool all_records = false) {
     const fl::Shape sh = fl::shape_for(g->n, g->terrains > 1);
     a.walk_grid = fl::walk_grid(sh.walk_per_sm);
     a.low_ilp = sh.low_ilp;
-    a.kahn_ilp = fl::tuning().kahn_ilp > 0 ? fl::tuning().kahn_ilp : kKahnIlp;
     a.sized_grids = g->sized_grids >= 0 ? g->sized_grids != 0 : sh.sized_grids;
     a.rec = g->d_rec;
     a.info = g->d_info;
@@ -1855,8 +1850,6 @@ int fl_set_tuning(const char* name, int64_t value) {
     const std::string k = name ? name : "";
     if (k == "low_ilp" && (value == -1 || value == 1 || value == 2 || value == 4)) {
         t.low_ilp = (int)value;
-    } else if (k == "kahn_ilp" && (value == -1 || value == 1 || value == 2)) {
-        t.kahn_ilp = (int)value;
     } else if (k == "walk_per_sm" && value >= -1 && value <= 64) {
         t.walk_per_sm = (int)value;
     } else if (k == "sized_grids" && value >= -1 && value <= 1) {
@@ -1877,7 +1870,6 @@ int64_t fl_get_tuning(const char* name) {
     const fl::Tuning& t = fl::tuning();
     const std::string k = name ? name : "";
     if (k == "low_ilp") return t.low_ilp;
-    if (k == "kahn_ilp") return t.kahn_ilp;
     if (k == "walk_per_sm") return t.walk_per_sm;
     if (k == "kahn_min_width") return t.kahn_min_width;
     if (k == "gpu_rank") return t.gpu_rank ? 1 : 0;

@@ -229,7 +229,6 @@ uint64_t fl_graph_host_syncs(const fl_graph* g);
  * fl_schedule_entry); fl_set_tuning overrides them process-wide, -1 restoring the
  * schedule:
  *   "low_ilp"        top-down Kahn rounds, sites in flight per thread: 1, 2 or 4
- *   "kahn_ilp"       bottom-up Kahn rounds, sites in flight per thread: 1 or 2
  *   "walk_per_sm"    chain walker blocks per SM, 1 .. 64 (at most what fits), 0: all that fit
  *   "kahn_min_width" Kahn rounds stop below this frontier width (where the chain walks
  *                    take over), 256 .. 2^24, or 0 for n / 512 clamped to [8192, 65536];
@@ -238,8 +237,8 @@ uint64_t fl_graph_host_syncs(const fl_graph* g);
  *                    rest of the GPU to other streams' solves), 0: whole-GPU grids
  *   "gpu_rank"       1: the lake heap's order computed on the GPU where lengths decide it
  *                    (the host heap otherwise), 0: always the host heap
- * Change them only while no solve runs.  FL_LOW_ILP, FL_KAHN_ILP, FL_WALK_PER_SM,
- * FL_KAHN_MIN_WIDTH, FL_SIZED_GRIDS and FL_GPU_RANK in the environment set them at load. */
+ * Change them only while no solve runs.  FL_LOW_ILP, FL_WALK_PER_SM, FL_KAHN_MIN_WIDTH,
+ * FL_SIZED_GRIDS and FL_GPU_RANK in the environment set them at load. */
 int fl_set_tuning(const char* name, int64_t value);
 int64_t fl_get_tuning(const char* name);   /* -2 for an unknown name */
 /* This model's cooperative grids: 1 cut to its size, 0 the whole GPU, -1 as the
