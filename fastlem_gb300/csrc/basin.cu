@@ -114,48 +114,9 @@ __global__ void k_collect_leaves(uint32_t n, const uint32_t* __restrict__ pendin
         [&](uint32_t v, uint32_t pos) { order[pos] = v; });
 }
 
-// Kahn round 0, the leaves, one thread per leaf at full occupancy: the cooperative
-// rounds kernel holds a few blocks per SM, which would take the millions of leaves of a
-// large terrain in dozens of dependent tiles per block.  A leaf's drainage area is its
-// cell area; the round-1 frontier is appended after the leaves, where the rounds kernel
-// expects it, and meta[kMetaLeavesDone] tells that kernel to start at round 1.  Nothing
-// runs when the leaves are fewer than the stop width (the rounds kernel then stops at
-// round 0).
-__global__ void k_kahn_leaves(uint32_t n, const uint32_t* __restrict__ next,
-                              const double* __restrict__ area, double* __restrict__ A,
-                              uint32_t* pending, uint32_t* __restrict__ hgt, uint32_t* order,
-                              uint64_t* __restrict__ rtime, uint32_t min_width, uint32_t* meta,
-                              int* flags) {
-    const uint32_t nl = meta[kMetaLeaves];
-    if (nl == 0 || nl < min_width) return;
-    const uint32_t base = blockIdx.x * blockDim.x;
-    if (base >= nl) return;                              // block-uniform
-    if (base == 0 && threadIdx.x == 0) {
-        meta[kMetaLeavesDone] = 1;
-        rtime[0] = global_ns();
-    }
-    const uint32_t idx = base + threadIdx.x;
-    bool ready = false;
-    uint32_t p = 0;
-    if (idx < nl) {
-        const uint32_t v = __ldcg(&order[idx]);
-        A[v] = area[v];
-        hgt[v] = 0;
-        p = next[v];
-        ready = p != v && atomicSub(&pending[p], 1u) == 1u;
-    }
-    uint32_t pos = block_append(&meta[kMetaCnt0], ready);
-    if (pos != kNone) {
-        pos += nl;
-        if (pos < n) order[pos] = p;
-        else set_error(flags, kErrForest);
-    }
-}
-
 // Kahn rounds.  order[0, nleaves) holds the leaves; rounds append the next frontier
 // after the current one.  Writes hgt (round) and A of processed sites, the round
-// offsets roff[0..r_stop+1] and meta[kMetaRStop] = r_stop.  Starts at round 1 when
-// k_kahn_leaves took round 0.
+// offsets roff[0..r_stop+1] and meta[kMetaRStop] = r_stop.
 __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
                        const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
                        const double* __restrict__ area, double* A, uint32_t* pending,
@@ -169,12 +130,6 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
     if (gtid == 0) {
         roff[0] = 0;
         roff[1] = end;
-    }
-    if (meta[kMetaLeavesDone]) {                         // round 0 is done
-        beg = end;
-        end += meta[kMetaCnt0];
-        r = 1;
-        if (gtid == 0) roff[2] = end;
     }
     while (true) {
         if (gtid == 0) rtime[r] = global_ns();
@@ -1451,12 +1406,11 @@ k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
                    write_rec);
     };
     Site cur{};
-    if (rs > 1 && roff[rs - 1] + gtid < roff[rs]) inputs(order[roff[rs - 1] + gtid], cur);
-    // rounds rs - 1 .. 1; round 0 (the leaves) is k_low_leaves'
-    for (uint32_t r = rs; r-- > 1;) {
+    if (rs > 0 && roff[rs - 1] + gtid < roff[rs]) inputs(order[roff[rs - 1] + gtid], cur);
+    for (uint32_t r = rs; r-- > 0;) {
         const uint32_t b = roff[r], e = roff[r + 1];
-        const bool write_rec = true;
-        const uint32_t nidx = (r > 1 && roff[r - 1] + gtid < b) ? roff[r - 1] + gtid : kNone;
+        const bool write_rec = r > 0 || all_records;
+        const uint32_t nidx = (r > 0 && roff[r - 1] + gtid < b) ? roff[r - 1] + gtid : kNone;
         const uint32_t nv = nidx != kNone ? order[nidx] : kNone;   // next round, in flight
         uint32_t i = b + gtid;
         if (i < e) {                                   // the prefetched first site
@@ -1485,36 +1439,6 @@ k_low_top_down(TopDown td, const uint32_t* __restrict__ order,
         if (nv != kNone) inputs(nv, cur);
         if (!grid_barrier(td.flags)) return;
         if (gtid == 0) rtime[rs - r] = global_ns();
-    }
-    block_flag(td.flags, kChanged, changed);
-}
-
-// Top-down round 0, the leaves, one thread per leaf at full occupancy after the rounds
-// above them: each takes its receiver's record; leaves write no record of their own
-// (nobody reads it) unless every record is read back.
-template <bool kSlope>
-__global__ void k_low_leaves(TopDown td, const uint32_t* __restrict__ order,
-                             const uint32_t* __restrict__ roff, uint64_t* __restrict__ rtime,
-                             const uint32_t* meta, bool all_records) {
-    if (ld_acquire(&td.flags[kError])) return;
-    const uint32_t rs = meta[kMetaRStop];
-    if (rs == 0) return;
-    const uint32_t nl = roff[1];
-    const uint32_t base = blockIdx.x * blockDim.x;
-    if (base >= nl) return;                              // block-uniform
-    if (base == 0 && threadIdx.x == 0) rtime[rs] = global_ns();
-    const uint32_t idx = base + threadIdx.x;
-    bool changed = false;
-    if (idx < nl) {
-        const uint32_t v = order[idx];
-        const uint32_t p = td.next[v];
-        const bool root = p == v;
-        const TRec rp = root ? TRec{} : load_rec(&td.rec[p]);
-        const double tn = kSlope ? td.tanms[v] : __longlong_as_double(0x7ff8000000000000ll);
-        const double dist = kSlope ? td.rlen[v] : 1.0;
-        double en;
-        settle_own(td, v, root, rp, td.w[v], td.uu[v], tn, dist, __ldcg(&td.elev[v]),
-                   root && td.outlet[v] != 0, &en, &changed, all_records);
     }
     block_flag(td.flags, kChanged, changed);
 }
@@ -1627,8 +1551,6 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     // Kahn rounds: order 4 + next 4 + row 8 + area 8 + A 8 + hgt 4 + pending 4 per site,
     // col 4 + next 4 per slot, donor areas 8 per site
     hk.begin(hk.ctx);
-    k_kahn_leaves<<<nb, kThreads, 0, st>>>(n, a.next, a.area, a.A, a.pending, a.hgt, a.order,
-                                           a.rtime, a.kahn_min_width, a.meta, a.flags);
     e = coop_launch(k_kahn, g_kahn, kThreads, st, n, a.row, a.col, a.next, a.area, a.A, a.pending,
                     a.hgt, a.order, a.roff, a.rtime, a.max_rounds, a.kahn_min_width, a.meta,
                     a.flags);
@@ -1739,19 +1661,6 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
         e = coop_launch_ptr(kern, sized_grid(sz, coop_grid(kern, blk, 2048 / blk), n, blk * 16ull), blk, st, td,
                             (const uint32_t*)a.order, (const uint32_t*)a.roff,
                             a.rtime + a.max_rounds + 1, (const uint32_t*)a.meta, a.all_records);
-        if (e == cudaSuccess) {
-            if (a.slope)
-                k_low_leaves<true><<<nb, kThreads, 0, st>>>(td, (const uint32_t*)a.order,
-                                                            (const uint32_t*)a.roff,
-                                                            a.rtime + a.max_rounds + 1,
-                                                            (const uint32_t*)a.meta, a.all_records);
-            else
-                k_low_leaves<false><<<nb, kThreads, 0, st>>>(td, (const uint32_t*)a.order,
-                                                             (const uint32_t*)a.roff,
-                                                             a.rtime + a.max_rounds + 1,
-                                                             (const uint32_t*)a.meta, a.all_records);
-            e = cudaGetLastError();
-        }
     }
     hk.end(hk.ctx, kcLowDown, 112.0 * n);
     return e;

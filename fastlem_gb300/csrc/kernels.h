@@ -101,7 +101,6 @@ enum Meta {
     kMetaUpSlowHi,
     kMetaDownSlow,     // (2 words, u64) slowest top-down chain, packed by pack_chain_stat
     kMetaDownSlowHi,
-    kMetaLeavesDone,   // round 0 (the leaves) ran in its own full-occupancy kernel
     kMetaCount
 };
 static_assert(kMetaUpSlow % 2 == 0 && kMetaDownSlow % 2 == 0, "u64 meta words must be aligned");
