@@ -98,19 +98,29 @@ __device__ __forceinline__ double pull_area(uint32_t v, const uint32_t* __restri
     return a;
 }
 
+// Packed terrains: a terrain whose first unchanged iteration is recorded sits at its
+// fixed point; another pass over it would reproduce its values, so its sites take no
+// part in the basin pass (they stay out of the leaves, the rounds and the skeleton,
+// and keep their areas, records and elevations).
+__device__ __forceinline__ bool settled(const uint32_t* tid, const uint32_t* titer, uint32_t v) {
+    return tid && titer[tid[v]] != 0;
+}
+
 __global__ void k_count_donors(uint32_t n, const uint32_t* __restrict__ next,
-                               uint32_t* __restrict__ pending) {
+                               uint32_t* __restrict__ pending, const uint32_t* __restrict__ tid,
+                               const uint32_t* __restrict__ titer) {
     uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
+    if (v >= n || settled(tid, titer, v)) return;
     uint32_t p = next[v];
     if (p != v) atomicAdd(&pending[p], 1u);
 }
 
 // Leaves in site order per block range (one reservation per block).
 __global__ void k_collect_leaves(uint32_t n, const uint32_t* __restrict__ pending,
-                                 uint32_t* __restrict__ order, uint32_t* __restrict__ counter) {
+                                 uint32_t* __restrict__ order, uint32_t* __restrict__ counter,
+                                 const uint32_t* __restrict__ tid, const uint32_t* __restrict__ titer) {
     block_range_compact(
-        n, counter, [&](uint32_t v) { return pending[v] == 0; },
+        n, counter, [&](uint32_t v) { return pending[v] == 0 && !settled(tid, titer, v); },
         [&](uint32_t v, uint32_t pos) { order[pos] = v; });
 }
 
@@ -182,9 +192,10 @@ struct Ranks {
 
 __global__ void k_s_collect(uint32_t n, const uint32_t* __restrict__ hgt,
                             uint32_t* __restrict__ sid, uint32_t* __restrict__ slist,
-                            uint32_t* meta) {
+                            uint32_t* meta, const uint32_t* __restrict__ tid,
+                            const uint32_t* __restrict__ titer) {
     block_range_compact(
-        n, &meta[kMetaNs], [&](uint32_t v) { return hgt[v] == kNone; },
+        n, &meta[kMetaNs], [&](uint32_t v) { return hgt[v] == kNone && !settled(tid, titer, v); },
         [&](uint32_t v, uint32_t k) {
             sid[v] = k;
             slist[k] = v;
@@ -1544,8 +1555,10 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     cudaMemsetAsync(a.pending, 0, n * 4ull, st);
     cudaMemsetAsync(a.hgt, 0xff, n * 4ull, st);
     cudaMemsetAsync(a.meta, 0, kMetaCount * 4ull, st);
-    k_count_donors<<<nb, kThreads, 0, st>>>(n, a.next, a.pending);
-    k_collect_leaves<<<g_compact, kRoundBlock, 0, st>>>(n, a.pending, a.order, a.meta + kMetaLeaves);
+    const uint32_t* titer = a.tid ? a.titer : nullptr;
+    k_count_donors<<<nb, kThreads, 0, st>>>(n, a.next, a.pending, a.tid, titer);
+    k_collect_leaves<<<g_compact, kRoundBlock, 0, st>>>(n, a.pending, a.order, a.meta + kMetaLeaves,
+                                                        a.tid, titer);
     hk.end(hk.ctx, kcBasinBuild, 20.0 * n);
 
     // Kahn rounds: order 4 + next 4 + row 8 + area 8 + A 8 + hgt 4 + pending 4 per site,
@@ -1558,7 +1571,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     if (e != cudaSuccess) return e;
 
     hk.begin(hk.ctx);
-    k_s_collect<<<g_compact, kRoundBlock, 0, st>>>(n, a.hgt, a.sid, a.slist, a.meta);
+    k_s_collect<<<g_compact, kRoundBlock, 0, st>>>(n, a.hgt, a.sid, a.slist, a.meta, a.tid, titer);
     k_s_designate<<<gs, kThreads, 0, st>>>(a.row, a.col, a.next, a.hgt, a.A, a.slist, a.desig,
                                            a.meta);
     k_s_link<<<gs, kThreads, 0, st>>>(a.next, a.desig, a.hgt, a.sid, a.slist, a.sptr0, a.sdist0,

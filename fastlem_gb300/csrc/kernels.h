@@ -163,9 +163,11 @@ struct BasinArgs {
     uint32_t* meta;
     int* flags;
     // packed terrains (batched form): terrain of each site, per-terrain "elevation
-    // changed" words; both null for a single terrain
+    // changed" words and first unchanged iteration (nonzero: the terrain is at its fixed
+    // point and its sites take no part in the pass); all null for a single terrain
     const uint32_t* tid;
     int* tchg;
+    const uint32_t* titer;
     // skeleton
     uint32_t* sid;
     uint32_t* slist;
@@ -224,9 +226,12 @@ struct Hooks {
 // Sets the message fl_last_error() returns on this thread.
 void set_last_error(const char* msg);
 
+// Packed terrains: sites of a terrain with titer[tid[v]] != 0 (converged) are left as
+// they are (tid / titer null: every site is scanned).
 void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const uint32_t* col,
                       const double* len, const float* ilen, const double* elev,
-                      const uint8_t* outlet, uint32_t* next, double* rlen, int* flags);
+                      const uint8_t* outlet, uint32_t* next, double* rlen, int* flags,
+                      const uint32_t* tid = nullptr, const uint32_t* titer = nullptr);
 // ilen[s] = 1/len[s] in f32 (NaN where not a normal f32), for launch_receivers.
 void launch_inv_len(cudaStream_t st, uint64_t nnz, const double* len, float* ilen);
 

@@ -177,11 +177,13 @@ __global__ void k_receivers(uint32_t n, const uint32_t* __restrict__ row,
                             const uint32_t* __restrict__ col, const double* __restrict__ len,
                             const float* __restrict__ ilen, const double* __restrict__ elev,
                             const uint8_t* __restrict__ outlet, uint32_t* __restrict__ next,
-                            double* __restrict__ rlen, int* __restrict__ flags) {
+                            double* __restrict__ rlen, int* __restrict__ flags,
+                            const uint32_t* __restrict__ tid, const uint32_t* __restrict__ titer) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool lake = false, went_exact = false, scan = false;
     uint32_t s0 = 0, s1 = 0;
-    if (i < n) {
+    // a converged packed terrain keeps its routed receivers
+    if (i < n && !(tid && titer[tid[i]])) {
         if (outlet[i]) {
             next[i] = i;
             rlen[i] = 1.0;
@@ -212,9 +214,10 @@ __global__ void k_inv_len(uint64_t nnz, const double* __restrict__ len, float* _
 
 void launch_receivers(cudaStream_t st, uint32_t n, const uint32_t* row, const uint32_t* col,
                       const double* len, const float* ilen, const double* elev,
-                      const uint8_t* outlet, uint32_t* next, double* rlen, int* flags) {
-    k_receivers<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(n, row, col, len, ilen, elev,
-                                                                     outlet, next, rlen, flags);
+                      const uint8_t* outlet, uint32_t* next, double* rlen, int* flags,
+                      const uint32_t* tid, const uint32_t* titer) {
+    k_receivers<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+        n, row, col, len, ilen, elev, outlet, next, rlen, flags, tid && titer ? tid : nullptr, titer);
 }
 
 void launch_inv_len(cudaStream_t st, uint64_t nnz, const double* len, float* ilen) {

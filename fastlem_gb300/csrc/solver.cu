@@ -1123,7 +1123,8 @@ int set_outlets(fl_graph* g, const std::vector<uint32_t>& outlets, bool need_ran
 int enqueue_receivers(fl_graph* g) {
     FL_LAUNCH(g, kcReceivers, 25.0 * g->n + 20.0 * g->nnz,
               fl::launch_receivers(g->stream, g->n, g->d_row, g->d_col, g->d_len, g->d_ilen,
-                                   g->d_elev, g->d_outlet, g->d_next, g->d_rlen, g->d_flags));
+                                   g->d_elev, g->d_outlet, g->d_next, g->d_rlen, g->d_flags,
+                                   g->d_tid, g->d_titer));
     FL_CU(cudaGetLastError());
     return FL_OK;
 }
@@ -1227,6 +1228,7 @@ int enqueue_basin_pass(fl_graph* g, bool all_records = false) {
     a.flags = g->d_flags;
     a.tid = g->d_tid;
     a.tchg = g->d_tchg;
+    a.titer = g->d_titer;
     a.sid = g->d_sid;
     a.slist = g->d_slist;
     a.desig = g->d_desig;

@@ -98,3 +98,18 @@ def test_batch_of_one_and_repeated_generate(cases):
         got = bg.generate()[0].elevations()
         assert np.array_equal(bits(got), bits(we))
         assert int(bg.last_terrain_iterations[0]) == wi
+
+
+def test_batch_to_convergence_matches_solo(cases):
+    """Without a bound every terrain runs to its own first unchanged iteration; the
+    terrains that settle first sit out the later iterations of the packed solve (their
+    sites take no part in the passes) and must still equal their solo solves."""
+    picked = [cases[i] for i in (0, 1, 4, 5)]        # fastlem's default uplift: they settle
+    want = [solo(m, p) for m, p in picked]
+    assert len(set(wi for _, wi in want)) > 1         # they settle at different iterations
+    bg = BatchGenerator().set_models([m for m, _ in picked]).set_parameters([p for _, p in picked])
+    got = bg.generate()
+    for t, ((we, wi), ge) in enumerate(zip(want, got)):
+        assert np.array_equal(bits(ge.elevations()), bits(we)), f"terrain {t}"
+        assert int(bg.last_terrain_iterations[t]) == wi, f"terrain {t} iterations"
+    assert bg.last_iterations == max(wi for _, wi in want)
