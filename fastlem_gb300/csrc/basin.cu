@@ -213,13 +213,39 @@ __global__ void k_s_designate(const uint32_t* __restrict__ row, const uint32_t* 
         uint32_t p = slist[k];
         uint32_t best = kNone;
         double ba = 0.0;
-        for (uint32_t s = row[p]; s < row[p + 1]; ++s) {
-            uint32_t d = col[s];
-            if (d == p || next[d] != p || hgt[d] != kNone) continue;
-            double a = A[d];
-            if (best == kNone || a > ba) {
-                best = d;
-                ba = a;
+        const uint32_t s0 = row[p], s1 = row[p + 1];
+        if (s1 - s0 <= (uint32_t)kRowFast) {
+            // columns, receivers, then the donors' heights and areas: a phase at a time
+            const uint32_t deg = s1 - s0;
+            uint32_t dd[kRowFast], donm = 0, skelm = 0;
+            double av[kRowFast];
+#pragma unroll
+            for (int j = 0; j < kRowFast; ++j)
+                if ((uint32_t)j < deg) dd[j] = col[s0 + j];
+#pragma unroll
+            for (int j = 0; j < kRowFast; ++j)
+                if ((uint32_t)j < deg && dd[j] != p && next[dd[j]] == p) donm |= 1u << j;
+#pragma unroll
+            for (int j = 0; j < kRowFast; ++j)
+                if ((donm >> j) & 1u) {
+                    if (hgt[dd[j]] == kNone) skelm |= 1u << j;
+                    av[j] = A[dd[j]];
+                }
+#pragma unroll
+            for (int j = 0; j < kRowFast; ++j)
+                if ((skelm >> j) & 1u && (best == kNone || av[j] > ba)) {
+                    best = dd[j];
+                    ba = av[j];
+                }
+        } else {
+            for (uint32_t s = s0; s < s1; ++s) {
+                uint32_t d = col[s];
+                if (d == p || next[d] != p || hgt[d] != kNone) continue;
+                double a = A[d];
+                if (best == kNone || a > ba) {
+                    best = d;
+                    ba = a;
+                }
             }
         }
         desig[p] = best;
@@ -548,21 +574,17 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
         // reverse row order: additions before the predecessor fold into pre, up to
         // kMaxPost after it are replayed by the walk; anything else keeps the whole
         // donor list
-        const uint32_t s0 = row[v], s1 = row[v + 1];
-        for (uint32_t s = s1; s-- > s0;) {
-            uint32_t d = col[s];
-            if (d == v || next[d] != v) continue;
+        auto visit = [&](uint32_t d, bool skel, double val) {     // donor d
             ++ndon;
             if (d == heavy) {
                 seen_heavy = true;
-                continue;
+                return;
             }
-            if (hgt[d] == kNone) {          // another chain's bottom: pushed at walk time
+            if (skel) {                     // another chain's bottom: pushed at walk time
                 list = true;
-                continue;
+                return;
             }
-            if (list) continue;
-            double val = A[d];
+            if (list) return;
             if (!seen_heavy) {
                 a = __dadd_rn(a, val);
             } else if (np < kMaxPost) {
@@ -572,6 +594,36 @@ __global__ void k_s_prepare(uint32_t n_sites, const uint32_t* __restrict__ row,
                 ++np;
             } else {
                 list = true;
+            }
+        };
+        const uint32_t s0 = row[v], s1 = row[v + 1];
+        if (s1 - s0 <= (uint32_t)kRowFast) {
+            // columns, then receivers, then the donors' heights and areas, each phase's
+            // loads in flight together
+            const uint32_t deg = s1 - s0;
+            uint32_t dd[kRowFast], donm = 0, skelm = 0;
+            double av[kRowFast];
+#pragma unroll
+            for (int k = 0; k < kRowFast; ++k)
+                if ((uint32_t)k < deg) dd[k] = col[s0 + k];
+#pragma unroll
+            for (int k = 0; k < kRowFast; ++k)
+                if ((uint32_t)k < deg && dd[k] != v && next[dd[k]] == v) donm |= 1u << k;
+#pragma unroll
+            for (int k = 0; k < kRowFast; ++k)
+                if ((donm >> k) & 1u) {
+                    if (hgt[dd[k]] == kNone) skelm |= 1u << k;
+                    av[k] = A[dd[k]];
+                }
+#pragma unroll
+            for (int k = kRowFast - 1; k >= 0; --k)
+                if ((donm >> k) & 1u) visit(dd[k], (skelm >> k) & 1u, av[k]);
+        } else {
+            for (uint32_t s = s1; s-- > s0;) {
+                const uint32_t d = col[s];
+                if (d == v || next[d] != v) continue;
+                const bool skel = hgt[d] == kNone;
+                visit(d, skel, skel ? 0.0 : A[d]);
             }
         }
         uint32_t toff = 0;
@@ -1546,7 +1598,7 @@ cudaError_t basin_pass(const BasinArgs& a, cudaStream_t st, const Hooks& hk, uin
     const unsigned g_chain = sized_grid(sz, a.walk_grid, n, 4096, 16);
     const unsigned g_tree = sized_grid(sz, coop_grid((const void*)k_s_chain_tree, kThreads, 4), n / 16,
                                        kThreads * 4);
-    const unsigned gs = 152 * 4;   // grid-stride kernels over the skeleton
+    const unsigned gs = 152 * 8;   // grid-stride kernels over the skeleton
     Ranks rk{{a.sptr0, a.sptr1}, {a.sdist0, a.sdist1}};
     TopDown td{a.next, a.w, a.u, a.tanms, a.rlen, a.outlet, a.rec_t, a.elev, a.flags, a.tid, a.tchg};
     cudaError_t e;
