@@ -476,6 +476,8 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
     const uint32_t ns = meta[kMetaNs];
     // with a walker for every chain all chains run at once and their order is free
     const bool sort = nc > walkers;
+    // the pointer jumping's rotating "moved" words (k_s_rank's before)
+    if (gtid == 0) meta[kMetaJump0] = meta[kMetaJump1] = 0;
     for (uint32_t i = gtid; i <= ns; i += stride) hist[i] = 0;
     for (uint32_t c = gtid; c < nc; c += stride) {
         const uint32_t v = layout[coff[c]];
@@ -493,19 +495,27 @@ __global__ void k_s_chain_tree(const uint32_t* __restrict__ next, const uint32_t
         }
     }
     if (!grid_barrier(flags)) return;
-    // ceil(log2(nc)) + 1 rounds reach every root
+    // ceil(log2(nc)) + 1 rounds reach every root; the rounds stop earlier once no pointer
+    // moves (every pointer is then a root: the chain tree is shallow)
     int rounds = 1;
     while ((1u << (rounds - 1)) < nc && rounds < 32) ++rounds;
     uint32_t *pin = par0, *din = dep0, *pout = par1, *dout = dep1;
     for (int r = 0; r < rounds; ++r) {
+        const uint32_t* moved_w = &meta[kMetaJump0 + (r % 3)];
+        if (gtid == 0) meta[kMetaJump0 + ((r + 1) % 3)] = 0;
+        bool moved = false;
         for (uint32_t c = gtid; c < nc; c += stride) {
             const uint32_t p = pin[c];
-            pout[c] = pin[p];
+            const uint32_t pp = pin[p];
+            pout[c] = pp;
             dout[c] = p == c ? din[c] : din[c] + din[p];
+            moved |= pp != p;
         }
+        if (__syncthreads_or(moved) && threadIdx.x == 0) atomicOr(&meta[kMetaJump0 + (r % 3)], 1u);
         if (!grid_barrier(flags)) return;
         uint32_t* t = pin; pin = pout; pout = t;
         t = din; din = dout; dout = t;
+        if (ld_acquire_u(moved_w) == 0) break;
     }
     // root chains, consistency, and the subtree maxima start at the own depth
     uint32_t* maxd = dout;
