@@ -36,7 +36,9 @@ METRIC = "Msite-iters/s at 16M sites"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 10; 3 for the reference arm, whose steps take "
+                         "seconds each)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="16m",
@@ -60,7 +62,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="16M run: skip the batched (C4) and served (C5) summaries")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 3 if args.impl == "reference" else 10
+    return args
 
 
 class Dist:
@@ -96,7 +101,10 @@ class Dist:
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle-reason samples every 200 ms while running."""
+    """nvidia-smi clock / throttle-reason samples every 100 ms.  The sampler is started
+    (and its first sample awaited, so that nvidia-smi's start-up does not fall into the
+    timed region) before timing begins; summary() keeps the samples taken inside the
+    timed region (start() .. stop())."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -104,22 +112,36 @@ class ClockSampler:
     def __init__(self, gpus):
         self.gpus = gpus
         self.proc = None
-        self.lines = []
+        self.lines = []                 # (arrival time, line)
+        self.t0 = self.t1 = None
+        self.first = threading.Event()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=15)
         except OSError:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+            self.first.set()
+
+    def start(self):
+        self.t0 = time.perf_counter()
+
+    def stop(self):
+        self.t1 = time.perf_counter()
+        if self.proc:                   # one more sample covers the region's end
+            deadline = self.t1 + 0.3
+            while time.perf_counter() < deadline and not any(t >= self.t1 for t, _ in self.lines):
+                time.sleep(0.02)
 
     def __exit__(self, *a):
         if self.proc:
@@ -133,7 +155,14 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.t0 is not None and self.t1 is not None:
+            # samples taken in the region, plus the first one after it (it covers the
+            # region's last 100 ms)
+            inside = [(t, ln) for t, ln in lines if self.t0 <= t <= self.t1]
+            after = [(t, ln) for t, ln in lines if t > self.t1][:max(1, self.gpus)]
+            lines = inside + after
+        for _, ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9 or not f[0].isdigit() or int(f[0]) >= self.gpus:
                 continue
@@ -383,8 +412,9 @@ def bench_gpu(args, d):
     L.fl_graph_reset_stats(h)
     _lib.check(L.fl_graph_set_timing(h, 1))
     loop_ms, total_ms, iters = 0.0, 0.0, 0
-    d.barrier()
     with ClockSampler(max(1, args.gpus)) as clocks:
+        d.barrier()
+        clocks.start()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             gen.generate(out=out)
@@ -392,7 +422,8 @@ def bench_gpu(args, d):
             total_ms += gen.last_total_ms
             iters += gen.last_iterations
         wall_ms = 1000 * (time.perf_counter() - t0)
-    d.barrier()
+        clocks.stop()
+        d.barrier()
     _lib.check(L.fl_graph_set_timing(h, 0))
     stats = _lib.kernel_stats(h)
     basin = _lib.basin_stats(h)
@@ -534,16 +565,18 @@ def bench_batched(args, d, emit=True):
     identical = all(np.array_equal(a.view(np.uint64), b.elevations().view(np.uint64))
                     for a, b in zip(plain, got))
     # batched: K steps
-    d.barrier()
     loop_ms, total_ms = 0.0, 0.0
     with ClockSampler(max(1, args.gpus)) as clocks:
+        d.barrier()
+        clocks.start()
         t = time.perf_counter()
         for _ in range(args.steps):
             bg.generate()
             loop_ms += bg.last_loop_ms
             total_ms += bg.last_total_ms
         wall = time.perf_counter() - t
-    d.barrier()
+        clocks.stop()
+        d.barrier()
     loop_max = d.max(loop_ms)
     total_max = d.max(total_ms)
     if d.rank != 0:
@@ -638,8 +671,10 @@ def bench_served(args, d, emit=True):
     with ClockSampler(max(1, args.gpus)) as clocks:
         with TerrainServer(hbm_budget_bytes=120 * 10**9, slots=args.slots) as srv:
             ids = [srv.add_model(m) for m in w.models]
+            clocks.start()
             served, span = replay(lambda i, t0: srv.submit(ids[i], w.params[i], cap),
                                   lambda hs, t0: [srv.wait(h) for h in hs])
+            clocks.stop()
             stats = srv.stats()
     if d.rank != 0:
         return
