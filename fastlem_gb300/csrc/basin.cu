@@ -127,11 +127,10 @@ __global__ void k_collect_leaves(uint32_t n, const uint32_t* __restrict__ pendin
 // Kahn rounds.  order[0, nleaves) holds the leaves; rounds append the next frontier
 // after the current one.  Writes hgt (round) and A of processed sites, the round
 // offsets roff[0..r_stop+1] and meta[kMetaRStop] = r_stop.
-// Each warp walks its own contiguous range of a round with no block synchronisation:
-// the sites that become ready go to a warp-private buffer in shared memory, which the
-// warp appends to the next frontier with one atomic per flush (when nearly full, and at
-// the round's end), so the next frontier keeps the memory locality of this one.  The
-// frontier's order within a round changes nothing but memory order.
+// Each warp walks its own tiles of a round with no block synchronisation: the sites
+// that become ready go to a warp-private buffer in shared memory, which the warp
+// appends to the next frontier with one atomic per flush (when nearly full, and at the
+// round's end).  The frontier's order within a round changes nothing but memory order.
 constexpr uint32_t kKahnWarpBuf = 256;
 __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
                        const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
@@ -171,16 +170,11 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
             __syncwarp();
         };
         uint32_t nbuf = 0;                              // warp-uniform
-        // this warp's range of the round, whole tiles of 32
-        const uint32_t chunk = ((width + nwarps - 1) / nwarps + 31u) & ~31u;
-        const uint64_t lo64 = (uint64_t)beg + (uint64_t)wglob * chunk;
-        const uint32_t lo = (uint32_t)(lo64 < end ? lo64 : end);
-        const uint32_t hi = (uint32_t)(lo64 + chunk < end ? lo64 + chunk : end);
-        for (uint32_t base = lo; base < hi; base += 32) {
+        for (uint32_t base = beg + wglob * 32; base < end; base += nwarps * 32) {
             const uint32_t idx = base + lane;
             bool ready = false;
             uint32_t p = 0;
-            if (idx < hi) {
+            if (idx < end) {
                 uint32_t v = __ldcg(&order[idx]);
                 // round 0 is the leaves: no donors, the drainage area is the cell area
                 A[v] = (r == 0) ? area[v] : pull_area(v, row, col, next, area, A);
