@@ -127,23 +127,14 @@ __global__ void k_collect_leaves(uint32_t n, const uint32_t* __restrict__ pendin
 // Kahn rounds.  order[0, nleaves) holds the leaves; rounds append the next frontier
 // after the current one.  Writes hgt (round) and A of processed sites, the round
 // offsets roff[0..r_stop+1] and meta[kMetaRStop] = r_stop.
-// Each warp walks its own tiles of a round with no block synchronisation: the sites
-// that become ready go to a warp-private buffer in shared memory, which the warp
-// appends to the next frontier with one atomic per flush (when nearly full, and at the
-// round's end).  The frontier's order within a round changes nothing but memory order.
-constexpr uint32_t kKahnWarpBuf = 256;
 __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
                        const uint32_t* __restrict__ col, const uint32_t* __restrict__ next,
                        const double* __restrict__ area, double* A, uint32_t* pending,
                        uint32_t* __restrict__ hgt, uint32_t* order, uint32_t* roff,
                        uint64_t* __restrict__ rtime, uint32_t max_rounds, uint32_t min_width,
                        uint32_t* meta, int* flags) {
-    __shared__ uint32_t s_buf[kThreads / 32][kKahnWarpBuf];
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t wglob = gtid >> 5, nwarps = stride >> 5;
-    uint32_t* wbuf = s_buf[threadIdx.x >> 5];
     uint32_t beg = 0, end = ld_acquire_u(&meta[kMetaLeaves]);
     uint32_t r = 0;
     if (gtid == 0) {
@@ -156,22 +147,9 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
         if (width == 0 || width < min_width || r + 2 >= max_rounds) break;
         uint32_t* cnt = &meta[kMetaCnt0 + (r % 3)];
         if (gtid == 0) meta[kMetaCnt0 + ((r + 1) % 3)] = 0;
-        // appends the warp's m buffered sites after this round's frontier
-        auto flush = [&](uint32_t m) {
-            __syncwarp();
-            uint32_t b = 0;
-            if (lane == 0 && m) b = atomicAdd(cnt, m);
-            b = __shfl_sync(0xffffffffu, b, 0);
-            for (uint32_t i = lane; i < m; i += 32) {
-                const uint32_t pos = end + b + i;
-                if (pos < n) order[pos] = wbuf[i];
-                else set_error(flags, kErrForest);
-            }
-            __syncwarp();
-        };
-        uint32_t nbuf = 0;                              // warp-uniform
-        for (uint32_t base = beg + wglob * 32; base < end; base += nwarps * 32) {
-            const uint32_t idx = base + lane;
+        // block-uniform trip count: block_append synchronises the block
+        for (uint32_t tile = beg + blockIdx.x * blockDim.x; tile < end; tile += stride) {
+            const uint32_t idx = tile + threadIdx.x;
             bool ready = false;
             uint32_t p = 0;
             if (idx < end) {
@@ -182,15 +160,13 @@ __global__ void k_kahn(uint32_t n, const uint32_t* __restrict__ row,
                 p = next[v];
                 ready = p != v && atomicSub(&pending[p], 1u) == 1u;
             }
-            const unsigned bal = __ballot_sync(0xffffffffu, ready);
-            if (ready) wbuf[nbuf + __popc(bal & ((1u << lane) - 1u))] = p;
-            nbuf += __popc(bal);
-            if (nbuf > kKahnWarpBuf - 32) {
-                flush(nbuf);
-                nbuf = 0;
+            uint32_t pos = block_append(cnt, ready);
+            if (pos != kNone) {
+                pos += end;
+                if (pos < n) order[pos] = p;
+                else set_error(flags, kErrForest);
             }
         }
-        flush(nbuf);
         if (!grid_barrier(flags)) return;
         beg = end;
         end = end + ld_acquire_u(cnt);
