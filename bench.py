@@ -522,7 +522,8 @@ def bench_gpu(args, d):
         sv = bench_served(ea, d, emit=False)
         line["served"] = {k: sv[k] for k in ("metric", "value", "unit", "latency_ms",
                                               "sequential_plain", "speedup_vs_sequential",
-                                              "identical_to_plain", "cpu_baseline", "server")}
+                                              "identical_to_plain", "cpu_baseline", "server",
+                                              "mean_in_service", "queue_ms")}
         line["served"]["config"] = sv["config"]
         it = bench_interp(ea, d, emit=False)
         line["interp"] = {k: it[k] for k in ("metric", "value", "unit", "e2e", "cpu_baseline",
