@@ -390,6 +390,7 @@ struct fl_graph {
     uint64_t dev_bytes = 0;   // device memory the model holds
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_status[2] = {nullptr, nullptr};   // an iteration's status copy is done
     // host copies used by the host-side lake-heap rank
     std::vector<uint32_t> h_row, h_col;
     std::vector<double> h_len;
@@ -506,6 +507,11 @@ int dalloc(T** p, uint64_t count) {
 
 // Page-locked 256-byte status blocks, recycled (freeing page-locked memory may
 // synchronise the device).
+// A page-locked status block: [0, kStatusSlot) for sync_status, then two slots of
+// flags + bookkeeping words for the pipelined iterations.
+constexpr uint32_t kStatusSlot = 64;
+static_assert(kNumFlags + kMetaCount <= kStatusSlot, "status slot too small");
+
 int* status_block_get() {
     std::lock_guard<std::mutex> lk(status_mu());
     auto& fl = status_free();
@@ -515,7 +521,8 @@ int* status_block_get() {
         return b;
     }
     void* p = nullptr;
-    if (cudaHostAlloc(&p, 256, cudaHostAllocPortable) != cudaSuccess) return nullptr;
+    if (cudaHostAlloc(&p, 3 * kStatusSlot * sizeof(int), cudaHostAllocPortable) != cudaSuccess)
+        return nullptr;
     return (int*)p;
 }
 void status_block_put(int* b) {
@@ -549,6 +556,8 @@ void free_graph(fl_graph* g) {
     }
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
+    for (cudaEvent_t e : g->ev_status)
+        if (e) cudaEventDestroy(e);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }
@@ -715,6 +724,17 @@ int sync_status(fl_graph* g, int* h, bool meta = false) {
 int clear_flags(fl_graph* g) {
     FL_CU(cudaMemsetAsync(g->d_flags, 0, 4 * sizeof(int), g->stream));
     FL_CU(cudaMemsetAsync(g->d_flags + kExact, 0, (kJump2 + 1 - kExact) * sizeof(int), g->stream));
+    return FL_OK;
+}
+
+// Copies this iteration's status words and bookkeeping into pipeline slot `slot`
+// behind its kernels.
+int enqueue_status(fl_graph* g, int slot) {
+    int* sb = g->h_status + kStatusSlot * (1 + slot);
+    FL_CU(cudaMemcpyAsync(sb, g->d_flags, kNumFlags * sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaMemcpyAsync(sb + kNumFlags, g->d_meta, kMetaCount * sizeof(uint32_t),
+                          cudaMemcpyDeviceToHost, g->stream));
+    FL_CU(cudaEventRecord(g->ev_status[slot], g->stream));
     return FL_OK;
 }
 
@@ -1294,6 +1314,17 @@ int finish_basin_pass(fl_graph* g, const int* h) {
     return FL_OK;
 }
 
+// Waits for the status copied into pipeline slot `slot` (one host synchronisation)
+// and takes it: h receives the status words, last_meta the bookkeeping.
+int take_status(fl_graph* g, int slot, int* h) {
+    FL_CU(cudaEventSynchronize(g->ev_status[slot]));
+    g->host_syncs++;
+    const int* sb = g->h_status + kStatusSlot * (1 + slot);
+    std::memcpy(h, sb, kNumFlags * sizeof(int));
+    std::memcpy(g->last_meta, sb + kNumFlags, sizeof g->last_meta);
+    return finish_basin_pass(g, h);
+}
+
 // Parameters into device order.  The uploads share one staging buffer; stream order
 // makes each copy wait for the previous gather, and a copy from pageable memory has
 // taken its data by the time it returns, so no host synchronisation is needed.
@@ -1376,14 +1407,26 @@ int generate_impl(fl_graph* g, uint32_t n_params, HostCols<const double> base,
         FL_CU(cudaMemsetAsync(g->d_tchg, 0, g->terrains * sizeof(int), g->stream));
         FL_CU(cudaMemsetAsync(g->d_titer, 0, g->terrains * sizeof(uint32_t), g->stream));
     }
-    // One blocking synchronisation per iteration, after the basin pass: whether an
-    // elevation changed (the loop's exit, generator.rs:207-209) and any device error.
+    // One host synchronisation per iteration, on the status of the iteration before:
+    // whether an elevation changed (the loop's exit, generator.rs:207-209) and any
+    // device error.  Iteration it is enqueued before the host waits for iteration
+    // it - 1's status (copied into one of two page-locked slots behind its kernels), so
+    // the device never waits for the host between iterations.  When iteration it - 1
+    // changed nothing, iteration it -- already queued -- recomputes the same fixed
+    // point (an iteration without a change leaves the elevations, hence everything the
+    // next one computes, as they were) and is not counted.  After a device error the
+    // queued work is drained before returning.
     // The lake stages are enqueued behind the receivers and skip themselves when the
     // receivers found no lake; only while the lake order for this outlet list is not on
     // the device yet does the host wait for the receivers' lake flag to compute it.
-    for (uint64_t it = 0; it < limit; ++it) {
-        ++iters;
-        int h[kNumFlags];
+    int h[kNumFlags];
+    auto drained = [&](int rc) {
+        cudaStreamSynchronize(g->stream);
+        return rc;
+    };
+    uint64_t it = 0;
+    bool settled = false;
+    for (; it < limit && !settled; ++it) {
         FL_TRY(clear_flags(g));
         FL_TRY(enqueue_receivers(g));
         bool lakes = true;
@@ -1401,12 +1444,21 @@ int generate_impl(fl_graph* g, uint32_t n_params, HostCols<const double> base,
         FL_TRY(enqueue_basin_pass(g));
         if (g->d_titer) {
             k_terrain_iters<<<blocks_for(g->terrains), kThreads, 0, g->stream>>>(
-                g->terrains, g->d_tchg, g->d_titer, iters);
+                g->terrains, g->d_tchg, g->d_titer, (uint32_t)(it + 1));
             FL_CU(cudaGetLastError());
         }
-        FL_TRY(sync_status(g, h, true));
-        FL_TRY(finish_basin_pass(g, h));
-        if (!h[kChanged]) break;
+        FL_TRY(enqueue_status(g, (int)(it & 1)));
+        if (it > 0) {
+            if (int rc = take_status(g, (int)((it - 1) & 1), h)) return drained(rc);
+            if (!h[kChanged]) {                       // iteration it - 1 was the last
+                iters = (uint32_t)it;
+                settled = true;
+            }
+        }
+    }
+    if (!settled && it > 0) {                         // the last iteration's status
+        if (int rc = take_status(g, (int)((it - 1) & 1), h)) return drained(rc);
+        iters = (uint32_t)it;
     }
     if (terrain_iters) {
         if (g->d_titer) {
@@ -1534,7 +1586,9 @@ int create_graph(uint32_t n, const uint32_t* row_ptr, const uint32_t* col, const
     cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { set_err("cudaStreamCreate", e); return fail(FL_ERR_CUDA); }
     t_alloc_stream = g->stream;
-    if (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess) {
+    if (cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g->ev_status[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g->ev_status[1], cudaEventDisableTiming) != cudaSuccess) {
         g_err = "cudaEventCreate failed";
         return fail(FL_ERR_CUDA);
     }
