@@ -205,3 +205,24 @@ def test_compiled_schedule_is_the_committed_one(fl_lib):
     want = [(c["max_sites"], int(c["packed"]), c["best"]["low_ilp"], c["best"]["walk_per_sm"],
              c["best"]["kahn_min_width"], int(c["best"].get("sized_grids", 0))) for c in classes]
     assert _lib.schedule() == want
+
+
+def test_tuning_knobs_reject_bad_values(fl_lib):
+    """fl_set_tuning takes only the documented names and ranges; fl_get_tuning reports -2
+    for an unknown name; a rejected call leaves the knob as it was."""
+    from fastlem_gb300 import _lib
+    from fastlem_gb300._lib import FL_ERR_INVALID_ARGUMENT
+    before = _lib.get_tuning()
+    for name, bad in (("low_ilp", 3), ("low_ilp", 8), ("walk_per_sm", 65), ("sized_grids", 2),
+                      ("gpu_rank", 2), ("kahn_min_width", 100), ("kahn_min_width", 1 << 25),
+                      ("no_such_knob", 1)):
+        assert fl_lib.fl_set_tuning(name.encode(), bad) == FL_ERR_INVALID_ARGUMENT, name
+    assert fl_lib.fl_set_tuning(None, 1) == FL_ERR_INVALID_ARGUMENT
+    assert fl_lib.fl_get_tuning(b"no_such_knob") == -2
+    assert _lib.get_tuning() == before
+    old = _lib.set_tuning(low_ilp=2, kahn_min_width=4096)
+    try:
+        assert _lib.get_tuning()["low_ilp"] == 2 and _lib.get_tuning()["kahn_min_width"] == 4096
+    finally:
+        _lib.set_tuning(**old)
+    assert _lib.get_tuning() == before
